@@ -1,0 +1,366 @@
+"""Benchmark: RVE solves/s of the Newton-CG homogenization on GB300.
+
+Workload (one "step" = one complete newton_cg solve): 128³ voxels, finite strain,
+MaterialLinearElastic1 with 40 seeded spherical inclusions (radii U[4,12] voxels,
+periodic wrap; E 210e9 in the spheres, 3e9 in the matrix, ν .3), applied
+F = I + 0.02 e1⊗e1, CG tol 1e-8, Newton tol 1e-6.  128 is even, so the cell uses
+the even-grid extension (Green operator zero at Nyquist k-points); the reference
+rejects even grids.
+
+value   mixed precision (FP32 inner CG / FFT / projection / tangent, FP64 Newton
+        level) solves/s with the microstructure resident in HBM (every field on the
+        device; 151 MB per field > 129 MB L2, so no L2 flush is needed between steps)
+e2e     the same solve through the public API from host buffers: cell construction
+        (host -> device upload of the microstructure), newton_cg, and the
+        OptimizeResult fields copied back (device -> host), wall clock
+fp64    the plain FP64 method on the same input, with the homogenised-stress error
+        of the mixed result against it
+roofline   the dominant kernel of one CG iteration, algorithmic bytes / CUDA-event
+        duration against the measured HBM copy bandwidth
+cpu_baseline  the NumPy/SciPy oracle (the reference's algorithm restated on the CPU)
+        on a bounded sample of the same workload, all host cores for its FFTs
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+# Newton and CG iteration counts of the FP64 method on this exact seeded input
+# (identical between the oracle and the GPU FP64 path, as the parity tests check);
+# the CPU runs time a bounded sample and scale by them
+REF_NEWTON_STEPS = None
+REF_CG_ITERS = None
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument('--gpus', type=int, default=1)
+    ap.add_argument('--steps', type=int, default=5)
+    ap.add_argument('--warmup', type=int, default=3)
+    ap.add_argument('--impl', default='ours', choices=['ours', 'reference'])
+    ap.add_argument('--n', type=int, default=128)
+    ap.add_argument('--fp64-steps', type=int, default=2)
+    ap.add_argument('--e2e-steps', type=int, default=2)
+    ap.add_argument('--cpu-cg-iters', type=int, default=4)
+    ap.add_argument('--no-cpu', action='store_true')
+    return ap.parse_args()
+
+
+def dist_init(args):
+    rank = int(os.environ.get('RANK', '0'))
+    world = int(os.environ.get('WORLD_SIZE', '1'))
+    local = int(os.environ.get('LOCAL_RANK', '0'))
+    return rank, world, local
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clock and throttle reasons during the timed region."""
+
+    FIELDS = 'index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,' \
+             'clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,' \
+             'clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap'
+
+    def __init__(self, gpu):
+        self.gpu = gpu
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix='.csv')
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(['nvidia-smi', '-i', str(self.gpu), '--query-gpu=' + self.FIELDS,
+                                          '--format=csv,noheader,nounits', '-lms', '200'],
+                                         stdout=open(self.path, 'w'), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ['hw_slowdown', 'hw_thermal_slowdown', 'sw_thermal_slowdown', 'sw_power_cap']
+        try:
+            for line in open(self.path):
+                f = [x.strip() for x in line.split(',')]
+                if len(f) < 9:
+                    continue
+                try:
+                    sm.append(float(f[1]))
+                    mx.append(float(f[2]))
+                except ValueError:
+                    continue
+                for nm, v in zip(names, f[5:9]):
+                    if v.lower().startswith('active'):
+                        reasons.add(nm)
+        except Exception:
+            pass
+        finally:
+            try:
+                os.unlink(self.path)
+            except Exception:
+                pass
+        if not sm:
+            return {'sm_mhz': None, 'sm_max_mhz': None, 'reasons': ['unsampled'], 'samples': 0}
+        return {'sm_mhz': statistics.median(sm), 'sm_max_mhz': max(mx), 'reasons': sorted(reasons),
+                'samples': len(sm)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, 'MEASURED_PEAKS.json')) as f:
+            d = json.load(f)
+        return float(d['hbm_gbs']), 'measured'
+    except Exception:
+        return 6800.0, 'fallback'
+
+
+def algorithmic_bytes(name, npx, nk, d2, s, tm):
+    """Bytes one launch of a CG-iteration kernel must move (per RHS)."""
+    u = npx * d2 * s        # one real field
+    spec = nk * d2 * 2 * s  # one half spectrum
+    return {
+        'last_axis_fwd_tangent': 3 * u + tm * npx + spec,  # r, p_old -> p; tangent data; spectrum out
+        'axis1_fwd': 2 * spec,
+        'green_axis0': 2 * spec,
+        'axis1_inv': 2 * spec,
+        'last_axis_inv_dot': spec + 2 * u,                 # spectrum in; p in; Ap out
+        'cg_update': 6 * u,                                # x, p, r, Ap in; x, r out
+        'cg_alpha': 0, 'cg_beta': 0,
+    }.get(name, 0)
+
+
+def cpu_baseline(w, newton_steps, cg_iters, nit):
+    """Oracle (NumPy/SciPy, FP64) on a bounded sample of the workload: one material
+    evaluation and `nit` CG iterations at full size, scaled to one solve by the FP64
+    method's Newton/CG counts."""
+    from oracle import muspectre_oracle as o
+    from muspectre_gb300 import workloads
+    o.FFT_WORKERS = os.cpu_count() or 1
+    cell = workloads.build_spheres_oracle(o, w)
+    d = 3
+    F = np.broadcast_to(np.eye(d) + w['load'], (cell.n_px, d, d)).copy()
+    cell.F = o.t2_to_vec(F)
+    t0 = time.perf_counter()
+    P, _ = cell.evaluate_stress_tangent()
+    rhs = -cell.apply_projection(P)
+    t_newton = time.perf_counter() - t0
+    solver = o.SolverCG(cell, 0.0, nit)
+    t0 = time.perf_counter()
+    try:
+        solver.solve(rhs)
+    except o.ConvergenceError:
+        pass  # tol 0: runs exactly nit iterations
+    t_cg = (time.perf_counter() - t0) / max(nit, 1)
+    t_solve = newton_steps * t_newton + cg_iters * t_cg
+    return {'solves_per_s': 1.0 / t_solve, 'pxit_per_s': cell.n_px / t_cg, 't_cg_iter_s': t_cg,
+            't_newton_step_s': t_newton, 'cores': o.FFT_WORKERS,
+            'sample': '1 material evaluation + rhs projection and %d CG iterations at %d^3 (FP64), scaled to '
+                      '%d Newton steps and %d CG iterations per solve' % (nit, w['res'][0], newton_steps, cg_iters)}
+
+
+def run_reference(args, rank, world):
+    """The reference's algorithm on the host CPU (the oracle; the C++ reference needs
+    Eigen and FFTW, absent here), same workload and metric."""
+    if rank != 0:
+        return
+    from muspectre_gb300 import workloads
+    w = workloads.spheres(args.n)
+    ns = REF_NEWTON_STEPS or 3
+    nc = REF_CG_ITERS or 600
+    vals = []
+    info = None
+    for step in range(args.warmup + args.steps):
+        info = cpu_baseline(w, ns, nc, max(1, args.cpu_cg_iters // 2))
+        if step >= args.warmup:
+            vals.append(info['solves_per_s'])
+    v = statistics.median(vals)
+    line = {'impl': 'reference', 'metric': 'RVE solves/s (Newton-CG, %d^3 finite-strain LE1)' % args.n, 'value': v,
+            'unit': 'solves/s', 'higher_is_better': True, 'n_gpus': args.gpus, 'steps': args.steps,
+            'warmup': args.warmup, 'ms_per_step': 1000.0 / v, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f64',
+            'data': 'synthetic (seeded spheres, seed %d)' % w['seed'],
+            'config': {'workload': 'spheres128_finite_le1', 'resolution': w['res'], 'nb_spheres': 40,
+                       'cg_tol': w['cg_tol'], 'newton_tol': w['newton_tol'], 'formulation': 'finite_strain'},
+            'cpu_baseline': {'value': v, 'unit': 'solves/s', 'cores': info['cores'], 'kind': 'port',
+                             'sample': info['sample']},
+            'e2e': {'value': v, 'unit': 'solves/s', 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_init(args)
+    if args.impl == 'reference':
+        run_reference(args, rank, world)
+        return
+    import torch
+    import muspectre_gb300 as mu
+    from muspectre_gb300 import workloads
+    torch.cuda.set_device(local)
+    mu._lib.lib().musg_set_device(local)
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group('nccl', device_id=torch.device('cuda', local))
+        pg = dist
+    stream = torch.cuda.Stream()
+
+    w = workloads.spheres(args.n)
+    cell = workloads.build_spheres_cell(mu, w)
+    cell.set_stream(stream.cuda_stream)
+    npx = cell.nb_pixels
+    mixed = mu.solvers.SolverCG(cell, w['cg_tol'], w['maxiter'], precision='mixed')
+    fp64 = mu.solvers.SolverCG(cell, w['cg_tol'], w['maxiter'], precision='fp64')
+
+    def solve(solver):
+        return mu.solvers.newton_cg(cell, w['load'], solver, w['newton_tol'], w['equil_tol'], return_fields=False)
+
+    def barrier():
+        torch.cuda.synchronize()
+        if pg:
+            pg.barrier()
+        torch.cuda.synchronize()
+
+    # ---------------- mixed precision, device resident (the headline)
+    for _ in range(args.warmup):
+        solve(mixed)
+    lat = []
+    c0 = mixed.get_counter()
+    barrier()
+    l0 = mu._lib.launch_count()
+    with Clocks(local) as clk:
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        for _ in range(args.steps):
+            e_a = torch.cuda.Event(enable_timing=True)
+            e_b = torch.cuda.Event(enable_timing=True)
+            e_a.record(stream)
+            r = solve(mixed)
+            e_b.record(stream)
+            lat.append((e_a, e_b))
+        ev1.record(stream)
+        barrier()
+    launches = mu._lib.launch_count() - l0
+    clocks = clk.summary()
+    t_ms = ev0.elapsed_time(ev1)
+    lat_ms = [a.elapsed_time(b) for a, b in lat]
+    cg_per_solve = (mixed.get_counter() - c0) / args.steps
+    newton_mixed = r.nb_it
+    if pg:
+        t = torch.tensor([t_ms], device='cuda')
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        t_ms = float(t.item())
+    value = world * args.steps / (t_ms / 1000.0)
+    stress_mixed = None
+
+    # per-kernel profile of one CG iteration (mixed) + roofline
+    prof = mixed.profile(5)
+    peak, peak_kind = measured_peaks()
+    d2 = 9
+    nk = (npx // w['res'][-1]) * (w['res'][-1] // 2 + 1)
+    tm = 4 * (9 + 9 + 2)  # F, S (FP32) and lambda, mu per pixel
+    kern = {}
+    for name, ms in prof.items():
+        b = algorithmic_bytes(name, npx, nk, d2, 4, tm)
+        kern[name] = {'ms': ms, 'gbs': (b / (ms * 1e-3) / 1e9) if ms > 0 and b else None, 'bytes': b}
+    tot = sum(v['ms'] for v in kern.values())
+    dom = max(kern, key=lambda k: kern[k]['ms'])
+    roof = {'bound': 'hbm', 'kernel': dom, 'achieved': kern[dom]['gbs'], 'peak': peak, 'unit': 'GB/s',
+            'frac': (kern[dom]['gbs'] / peak) if kern[dom]['gbs'] else None, 'traffic': None,
+            'peak_source': peak_kind, 'share': kern[dom]['ms'] / tot if tot else None,
+            'iteration_ms': tot,
+            'iteration_gbs': sum(v['bytes'] for v in kern.values()) / (tot * 1e-3) / 1e9 if tot else None,
+            'kernels': kern}
+
+    # ---------------- FP64 method on the same input
+    fp64_lat = []
+    for i in range(1 + args.fp64_steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r64 = mu.solvers.newton_cg(cell, w['load'], fp64, w['newton_tol'], w['equil_tol'], return_fields=(i == 0))
+        torch.cuda.synchronize()
+        if i == 0:
+            stress64 = r64.stress
+        else:
+            fp64_lat.append(time.perf_counter() - t0)
+    rm = mu.solvers.newton_cg(cell, w['load'], mixed, w['newton_tol'], w['equil_tol'])
+    stress_mixed = rm.stress
+    h64 = stress64.reshape(-1, 3, 3).mean(0)
+    hm = stress_mixed.reshape(-1, 3, 3).mean(0)
+    err = float(np.linalg.norm(hm - h64) / np.linalg.norm(h64))
+    fp64_sps = 1.0 / statistics.median(fp64_lat)
+    fp64_cg = r64.nb_fev  # cumulative counter: divide by solves done with this solver
+    fp64_cg_per_solve = fp64_cg / (1 + args.fp64_steps)
+
+    # ---------------- end to end through the public API from host buffers
+    e2e_t = []
+    h2d = npx * (1 + 2 * 8)  # material index byte + lambda, mu (FP64) per pixel
+    d2h = 2 * npx * d2 * 8
+    for i in range(args.e2e_steps + 1):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        c2 = workloads.build_spheres_cell(mu, w)
+        s2 = mu.solvers.SolverCG(c2, w['cg_tol'], w['maxiter'], precision='mixed')
+        r2 = mu.solvers.newton_cg(c2, w['load'], s2, w['newton_tol'], w['equil_tol'])
+        hs = r2.stress.reshape(-1, 3, 3).mean(0)
+        torch.cuda.synchronize()
+        if i > 0:
+            e2e_t.append(time.perf_counter() - t0)
+        del s2, c2
+    e2e_v = world / statistics.median(e2e_t)
+
+    line = {
+        'metric': 'RVE solves/s (FP32-mixed Newton-CG, %d^3 finite-strain LE1, 40 spheres)' % args.n,
+        'value': value, 'unit': 'solves/s', 'n_gpus': world, 'steps': args.steps, 'warmup': args.warmup,
+        'ms_per_step': t_ms / args.steps, 'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None,
+        'dtype': 'f32-mixed (f64 Newton)', 'data': 'synthetic (seeded spheres, seed %d)' % w['seed'],
+        'config': {'workload': 'spheres128_finite_le1', 'resolution': w['res'], 'nb_spheres': 40,
+                   'formulation': 'finite_strain', 'cg_tol': w['cg_tol'], 'newton_tol': w['newton_tol'],
+                   'even_grid_extension': True, 'l2': 'fields 151 MB > L2, no flush', 'parallelism': 'replicas'},
+        'latency_ms': {'p50': float(np.percentile(lat_ms, 50)), 'p99': float(np.percentile(lat_ms, 99))},
+        'newton_steps': newton_mixed, 'cg_iters_per_solve': cg_per_solve,
+        'pxit_per_s': value * npx * cg_per_solve / world * world,
+        'fp64': {'solves_per_s': fp64_sps, 'cg_iters_per_solve': fp64_cg_per_solve, 'newton_steps': r64.nb_it},
+        'speedup_vs_fp64': value / world / fp64_sps,
+        'stress_rel_err_vs_fp64': err,
+        'roofline': roof,
+        'clocks': clocks,
+        'gpu_launches': launches,
+        'e2e': {'value': e2e_v, 'unit': 'solves/s', 'h2d_bytes_per_step': h2d, 'd2h_bytes_per_step': d2h},
+    }
+    if rank == 0 and not args.no_cpu:
+        cb = cpu_baseline(w, r64.nb_it, int(round(fp64_cg_per_solve)), args.cpu_cg_iters)
+        line['cpu_baseline'] = {'value': cb['solves_per_s'], 'unit': 'solves/s', 'cores': cb['cores'], 'kind': 'port',
+                                'sample': cb['sample'], 'pxit_per_s': cb['pxit_per_s']}
+    if pg:
+        pg.barrier()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if pg:
+        pg.destroy_process_group()
+
+
+if __name__ == '__main__':
+    main()

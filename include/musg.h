@@ -1,0 +1,195 @@
+/*
+ * musg.h -- C ABI of the GB300-native µSpectre Newton-CG homogenization path.
+ *
+ * Plain C: opaque handles, plain pointers and sizes, int status codes.  Every
+ * function returns MUSG_OK (0) or an error code; the message of the last error of
+ * the calling thread is available through musg_last_error().  Arrays passed in or
+ * out are HOST memory in the reference's layouts unless the name says "_device":
+ *
+ *   - a strain/stress field ("vector" of nb_dof = nb_pixels*D*D doubles) is
+ *     pixel-major (AoS); pixel p, tensor entry A(i,j) sits at p*D*D + i + D*j
+ *     (Eigen column-major per pixel), pixels row-major with the last index fastest
+ *     (src/common/ccoord_operations.hh:151-192 of the reference);
+ *   - a tangent field holds D^4 doubles per pixel at (i+D*j) + D*D*(k+D*l)
+ *     (src/common/T4_map_proxy.hh:84-105);
+ *   - an FFT workspace holds nb_hermitian*nb_components complex values as
+ *     interleaved (re, im) doubles, AoS, the last axis halved to n/2+1
+ *     (src/fft/fftw_engine.cc:65-77).
+ *
+ * Each entry point names the reference interface it replaces.
+ */
+#ifndef MUSG_H
+#define MUSG_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes; the C++ layer maps them back onto the reference exception types */
+#define MUSG_OK 0
+#define MUSG_ERR_RUNTIME 1     /* std::runtime_error                                */
+#define MUSG_ERR_PROJECTION 2  /* ProjectionError (src/fft/projection_base.hh)      */
+#define MUSG_ERR_SOLVER 3      /* SolverError (src/solver/solver_common.hh:80-83)   */
+#define MUSG_ERR_CONVERGENCE 4 /* ConvergenceError (solver_common.hh:86-88)         */
+#define MUSG_ERR_SHAPE 5       /* size/shape mismatch (std::runtime_error upstream) */
+#define MUSG_ERR_CUDA 6        /* CUDA runtime failure                              */
+#define MUSG_ERR_MEMORY 7      /* device allocation failed                          */
+#define MUSG_ERR_ARGUMENT 8    /* invalid argument / handle                         */
+#define MUSG_ERR_NONFINITE 9   /* NaN/Inf met by a device kernel                    */
+
+/* Formulation (src/common/common.hh:149-153) */
+#define MUSG_FINITE_STRAIN 0
+#define MUSG_SMALL_STRAIN 1
+
+/* cell / projection creation flags */
+#define MUSG_FLAG_ALLOW_EVEN 1 /* lift the odd-grid guard: Ghat = 0 at Nyquist k-points */
+
+/* precision of the inner CG solve */
+#define MUSG_PRECISION_FP64 0  /* everything in FP64 (the reference method)          */
+#define MUSG_PRECISION_MIXED 1 /* FP32 CG/FFT/projection/tangent, FP64 Newton level   */
+
+/* material laws */
+#define MUSG_LAW_LE1 1  /* MaterialLinearElastic1:  params (E, nu)               */
+#define MUSG_LAW_LE2 2  /* MaterialLinearElastic2:  params (E, nu); per pixel D*D eigenstrain */
+#define MUSG_LAW_LE3 3  /* MaterialLinearElastic3:  per pixel (E, nu), full C   */
+#define MUSG_LAW_LE4 4  /* MaterialLinearElastic4:  per pixel (E, nu) -> (lambda, mu) */
+#define MUSG_LAW_HEP1 5 /* MaterialHyperElastoPlastic1: params (E, nu, tau_y0, H) */
+
+/* projection kinds */
+#define MUSG_PROJ_SMALL_STRAIN 0       /* ProjectionSmallStrain       */
+#define MUSG_PROJ_FINITE_STRAIN_FAST 1 /* ProjectionFiniteStrainFast  */
+#define MUSG_PROJ_FINITE_STRAIN 2      /* ProjectionFiniteStrain      */
+
+typedef struct musg_cell musg_cell;
+typedef struct musg_solver musg_solver;
+typedef struct musg_fft musg_fft;
+typedef struct musg_projection musg_projection;
+
+/* OptimizeResult (src/solver/solver_common.hh:50-67) without its two field arrays,
+ * which musg_newton_cg writes into caller buffers. */
+typedef struct musg_result_info {
+  int success;           /* OptimizeResult::success                    */
+  int status;            /* OptimizeResult::status                     */
+  unsigned nb_it;        /* Newton iterations of this load step        */
+  unsigned nb_fev;       /* cumulative CG iterations (solver counter)  */
+  char message[64];      /* OptimizeResult::message                    */
+} musg_result_info;
+
+/* -------------------------------------------------------------- library */
+const char *musg_last_error(void);
+int musg_version(void);
+/* number of visible CUDA devices (0 without a GPU; never fails on a CPU host) */
+int musg_device_count(int *count);
+/* device used by the objects the calling thread creates afterwards (one process per
+ * GPU; no counterpart in the reference, whose ranks are MPI processes) */
+int musg_set_device(int device);
+
+/* -------------------------------------------------------------- cell
+ * make_cell<D,D>(res, lengths, form) (src/cell/cell_factory.hh:93-105) and
+ * CellBase<D,D> (src/cell/cell_base.hh:241-526).  The projection is chosen by the
+ * formulation as upstream (cell_factory.hh:59-86): finite strain ->
+ * ProjectionFiniteStrainFast, small strain -> ProjectionSmallStrain; both reject
+ * even resolutions unless MUSG_FLAG_ALLOW_EVEN is given. */
+int musg_cell_create(int dim, const int *resolutions, const double *lengths,
+                     int formulation, int flags, musg_cell **out);
+int musg_cell_destroy(musg_cell *cell);
+/* Cell::get_nb_dof (cell_base.hh:115) and Cell::size (cell_base.hh:118) */
+int musg_cell_sizes(musg_cell *cell, long long *nb_dof, long long *nb_pixels);
+/* runs the cell's kernels on this CUDA stream (default: a stream the cell owns) */
+int musg_cell_set_stream(musg_cell *cell, void *cuda_stream);
+/* MaterialMuSpectre<...>::make(cell, name, params...) (material_muSpectre_base.hh:228-237) */
+int musg_material_create(musg_cell *cell, int law, const char *name,
+                         const double *params, int nb_params, int *material);
+/* add_pixel for many pixels at once (material_base.cc / LE2-4 .cc add_pixel):
+ * pixel indices are row-major linear indices; per_pixel holds stride values per
+ * pixel (LE2: D*D eigenstrain column-major; LE3/LE4: Young, Poisson), else NULL. */
+int musg_material_add_pixels(musg_cell *cell, int material,
+                             const long long *pixels, long long count,
+                             const double *per_pixel, int stride);
+/* MaterialBase::size */
+int musg_material_size(musg_cell *cell, int material, long long *count);
+/* CellBase::initialise (cell_base.cc:445-454): material coverage check, device
+ * upload of the microstructure, FFT plans.  Called implicitly by the first
+ * evaluation. plan_flags follows FFT_PlanFlags (estimate=0, measure=1, patient=2). */
+int musg_cell_initialise(musg_cell *cell, int plan_flags);
+/* CellBase::set_uniform_strain (cell_base.cc:110-112); strain is D*D column-major */
+int musg_cell_set_uniform_strain(musg_cell *cell, const double *strain);
+/* Cell::get_strain_vector / get_stress_vector (cell_base.cc:96-106): copies */
+int musg_cell_get_strain(musg_cell *cell, double *out);
+int musg_cell_set_strain(musg_cell *cell, const double *in);
+int musg_cell_get_stress(musg_cell *cell, double *out);
+/* Cell::evaluate_stress_tangent (cell_base.cc:129-146); either output may be NULL */
+int musg_cell_evaluate_stress_tangent(musg_cell *cell, double *stress_out,
+                                      double *tangent_out);
+/* Cell::apply_projection (cell_base.cc:202-208): in place on a host vector */
+int musg_cell_apply_projection(musg_cell *cell, double *vec);
+/* Cell::evaluate_projected_directional_stiffness (cell_base.cc:150-192) */
+int musg_cell_directional_stiffness(musg_cell *cell, const double *dF, double *dP);
+/* Cell::save_history_variables (cell_base.cc:458-462) */
+int musg_cell_save_history_variables(musg_cell *cell);
+
+/* -------------------------------------------------------------- solvers
+ * SolverCG(cell, tol, maxiter, verbose) (src/solver/solver_cg.hh:51-106) with the
+ * vectors resident on the device; precision selects the plain FP64 method or the
+ * mixed FP32-inner / FP64-outer variant. */
+int musg_solver_cg_create(musg_cell *cell, double tol, unsigned maxiter,
+                          int verbose, int precision, musg_solver **out);
+int musg_solver_destroy(musg_solver *solver);
+/* MUSG_PRECISION_MIXED only (no counterpart in the reference): the FP32 inner
+ * solve stops at max(tol, inner_tol), default 1e-5, and newton_cg refines in FP64 */
+int musg_solver_set_inner_tol(musg_solver *solver, double inner_tol);
+/* SolverBase::get_counter / reset_counter / has_converged (solver_base.hh:62-109) */
+int musg_solver_get_counter(musg_solver *solver, unsigned *counter);
+int musg_solver_reset_counter(musg_solver *solver);
+int musg_solver_has_converged(musg_solver *solver, int *converged);
+/* SolverCG::solve (solver_cg.cc:54-110): x_out = A^-1 rhs */
+int musg_solver_solve(musg_solver *solver, const double *rhs, double *x_out);
+
+/* newton_cg(cell, load_steps, solver, newton_tol, equil_tol, verbose)
+ * (src/solver/solvers.cc:44-217).  load_steps: nb_steps D*D column-major
+ * matrices.  grads / stresses (may be NULL) receive nb_steps*nb_dof doubles. */
+int musg_newton_cg(musg_cell *cell, const double *load_steps, int nb_steps,
+                   musg_solver *solver, double newton_tol, double equil_tol,
+                   int verbose, musg_result_info *infos, double *grads,
+                   double *stresses);
+
+/* ---------------------------------------------------------- instrumentation
+ * (no counterpart in the reference, which has no device)
+ * musg_launch_count: kernels launched by the library in this process, CUDA graph
+ *   replays counted per kernel node.
+ * musg_solver_profile: mean duration (ms, CUDA events on the cell's stream) of each
+ *   kernel of one CG iteration over `iterations` eager iterations started from the
+ *   cell's last projected residual; ms_out needs 8 entries; kernel names by
+ *   musg_solver_kernel_name.  Needs an evaluated tangent (after newton_cg). */
+int musg_launch_count(unsigned long long *count);
+int musg_solver_profile(musg_solver *solver, int iterations, double *ms_out, int *nb_kernels);
+const char *musg_solver_kernel_name(musg_solver *solver, int k);
+
+/* -------------------------------------------------------------- FFT engine
+ * FFTEngineBase<D> / FFTWEngine<D> (src/fft/fft_engine_base.hh:75-148,
+ * fftw_engine.cc:53-158): unnormalised r2c / c2r over nb_components interleaved
+ * components.  normalisation() is 1/nb_pixels. */
+int musg_fft_create(int dim, const int *resolutions, int nb_components, musg_fft **out);
+int musg_fft_destroy(musg_fft *fft);
+int musg_fft_forward(musg_fft *fft, const double *in, double *out_complex);
+int musg_fft_inverse(musg_fft *fft, const double *in_complex, double *out);
+
+/* -------------------------------------------------------------- projections
+ * ProjectionSmallStrain / ProjectionFiniteStrainFast / ProjectionFiniteStrain
+ * (src/fft/projection_*.cc; ProjectionBase projection_base.hh:99-161) */
+int musg_projection_create(int dim, const int *resolutions, const double *lengths,
+                           int kind, int flags, musg_projection **out);
+int musg_projection_destroy(musg_projection *proj);
+int musg_projection_apply(musg_projection *proj, double *vec);
+/* get_operator(): rows x nb_hermitian doubles, column-major as the reference
+ * stores Ghat (rows = D^4 for small/full finite strain, D for the fast variant);
+ * out may be NULL to query rows/cols */
+int musg_projection_get_operator(musg_projection *proj, double *out,
+                                 long long *rows, long long *cols);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MUSG_H */

@@ -1,0 +1,156 @@
+"""ctypes binding of libmusg.so (the C ABI declared in include/musg.h).
+
+The library is built in-tree by ``muspectre_gb300.build`` (``__graft_entry__.build()``).
+There is no CPU fallback: if the library is missing, every entry point raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, 'libmusg.so')
+
+# status codes (include/musg.h)
+OK, ERR_RUNTIME, ERR_PROJECTION, ERR_SOLVER, ERR_CONVERGENCE, ERR_SHAPE, ERR_CUDA, ERR_MEMORY, ERR_ARGUMENT, \
+    ERR_NONFINITE = range(10)
+FINITE_STRAIN, SMALL_STRAIN = 0, 1
+FLAG_ALLOW_EVEN = 1
+PRECISION_FP64, PRECISION_MIXED = 0, 1
+LAW_LE1, LAW_LE2, LAW_LE3, LAW_LE4, LAW_HEP1 = 1, 2, 3, 4, 5
+PROJ_SMALL_STRAIN, PROJ_FINITE_STRAIN_FAST, PROJ_FINITE_STRAIN = 0, 1, 2
+
+
+class ProjectionError(RuntimeError):
+    """ProjectionError (src/fft/projection_base.hh)."""
+
+
+class SolverError(RuntimeError):
+    """SolverError (src/solver/solver_common.hh:80-83)."""
+
+
+class ConvergenceError(SolverError):
+    """ConvergenceError (src/solver/solver_common.hh:86-88)."""
+
+
+class CudaError(RuntimeError):
+    """A CUDA runtime failure inside libmusg."""
+
+
+class ResultInfo(C.Structure):
+    _fields_ = [('success', C.c_int), ('status', C.c_int), ('nb_it', C.c_uint), ('nb_fev', C.c_uint),
+                ('message', C.c_char * 64)]
+
+
+_P = C.c_void_p
+_D = C.POINTER(C.c_double)
+_I = C.POINTER(C.c_int)
+_LL = C.POINTER(C.c_longlong)
+
+_SIGNATURES = {
+    'musg_last_error': (C.c_char_p, []),
+    'musg_version': (C.c_int, []),
+    'musg_device_count': (C.c_int, [_I]),
+    'musg_set_device': (C.c_int, [C.c_int]),
+    'musg_cell_create': (C.c_int, [C.c_int, _I, _D, C.c_int, C.c_int, C.POINTER(_P)]),
+    'musg_cell_destroy': (C.c_int, [_P]),
+    'musg_cell_sizes': (C.c_int, [_P, _LL, _LL]),
+    'musg_cell_set_stream': (C.c_int, [_P, _P]),
+    'musg_material_create': (C.c_int, [_P, C.c_int, C.c_char_p, _D, C.c_int, _I]),
+    'musg_material_add_pixels': (C.c_int, [_P, C.c_int, _LL, C.c_longlong, _D, C.c_int]),
+    'musg_material_size': (C.c_int, [_P, C.c_int, _LL]),
+    'musg_cell_initialise': (C.c_int, [_P, C.c_int]),
+    'musg_cell_set_uniform_strain': (C.c_int, [_P, _D]),
+    'musg_cell_get_strain': (C.c_int, [_P, _D]),
+    'musg_cell_set_strain': (C.c_int, [_P, _D]),
+    'musg_cell_get_stress': (C.c_int, [_P, _D]),
+    'musg_cell_evaluate_stress_tangent': (C.c_int, [_P, _D, _D]),
+    'musg_cell_apply_projection': (C.c_int, [_P, _D]),
+    'musg_cell_directional_stiffness': (C.c_int, [_P, _D, _D]),
+    'musg_cell_save_history_variables': (C.c_int, [_P]),
+    'musg_solver_cg_create': (C.c_int, [_P, C.c_double, C.c_uint, C.c_int, C.c_int, C.POINTER(_P)]),
+    'musg_solver_destroy': (C.c_int, [_P]),
+    'musg_solver_set_inner_tol': (C.c_int, [_P, C.c_double]),
+    'musg_solver_get_counter': (C.c_int, [_P, C.POINTER(C.c_uint)]),
+    'musg_solver_reset_counter': (C.c_int, [_P]),
+    'musg_solver_has_converged': (C.c_int, [_P, _I]),
+    'musg_solver_solve': (C.c_int, [_P, _D, _D]),
+    'musg_newton_cg': (C.c_int, [_P, _D, C.c_int, _P, C.c_double, C.c_double, C.c_int, C.POINTER(ResultInfo), _D,
+                                 _D]),
+    'musg_launch_count': (C.c_int, [C.POINTER(C.c_ulonglong)]),
+    'musg_solver_profile': (C.c_int, [_P, C.c_int, _D, _I]),
+    'musg_solver_kernel_name': (C.c_char_p, [_P, C.c_int]),
+    'musg_fft_create': (C.c_int, [C.c_int, _I, C.c_int, C.POINTER(_P)]),
+    'musg_fft_destroy': (C.c_int, [_P]),
+    'musg_fft_forward': (C.c_int, [_P, _D, _D]),
+    'musg_fft_inverse': (C.c_int, [_P, _D, _D]),
+    'musg_projection_create': (C.c_int, [C.c_int, _I, _D, C.c_int, C.c_int, C.POINTER(_P)]),
+    'musg_projection_destroy': (C.c_int, [_P]),
+    'musg_projection_apply': (C.c_int, [_P, _D]),
+    'musg_projection_get_operator': (C.c_int, [_P, _D, _LL, _LL]),
+}
+
+_lib = None
+
+
+def lib():
+    """The loaded library; raises when it has not been built (no fallback)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError('libmusg.so is not built (%s); run `python -c "import __graft_entry__ as g; g.build()"` '
+                               'or `python -m muspectre_gb300.build`' % LIB_PATH)
+        handle = C.CDLL(LIB_PATH)
+        for name, (res, args) in _SIGNATURES.items():
+            fn = getattr(handle, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = handle
+    return _lib
+
+
+def check(rc):
+    if rc == OK:
+        return
+    msg = lib().musg_last_error().decode('utf-8', 'replace')
+    if rc == ERR_PROJECTION:
+        raise ProjectionError(msg)
+    if rc == ERR_CONVERGENCE:
+        raise ConvergenceError(msg)
+    if rc == ERR_SOLVER:
+        raise SolverError(msg)
+    if rc in (ERR_CUDA, ERR_MEMORY):
+        raise CudaError(msg)
+    if rc == ERR_ARGUMENT:
+        raise ValueError(msg)
+    raise RuntimeError(msg)
+
+
+def dptr(a):
+    return a.ctypes.data_as(_D) if a is not None else None
+
+
+def iptr(a):
+    return a.ctypes.data_as(_I)
+
+
+def llptr(a):
+    return a.ctypes.data_as(_LL)
+
+
+def f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def launch_count():
+    n = C.c_ulonglong(0)
+    check(lib().musg_launch_count(C.byref(n)))
+    return n.value
+
+
+def device_count():
+    n = C.c_int(0)
+    check(lib().musg_device_count(C.byref(n)))
+    return n.value

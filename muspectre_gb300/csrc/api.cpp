@@ -1,0 +1,1111 @@
+// C ABI of libmusg (include/musg.h): cells, materials, SolverCG, newton_cg, the FFT
+// engine and the projections.  Host C++ drives the device kernels; every field
+// lives on the GPU and crosses to the host only at the API boundary (get_strain,
+// get_stress, OptimizeResult copies).
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "musg_internal.h"
+
+using namespace musg;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+template <typename F> int guard(F &&f) {
+  try {
+    f();
+    return MUSG_OK;
+  } catch (const Error &e) {
+    g_last_error = e.what();
+    return e.code;
+  } catch (const std::bad_alloc &) {
+    g_last_error = "host allocation failed";
+    return MUSG_ERR_MEMORY;
+  } catch (const std::exception &e) {
+    g_last_error = e.what();
+    return MUSG_ERR_RUNTIME;
+  }
+}
+
+void require(bool ok, int code, const std::string &msg) {
+  if (!ok) throw Error(code, msg);
+}
+
+// Hooke helpers (src/materials/materials_toolbox.hh:491-525)
+double lame_lambda(double E, double nu) { return E * nu / ((1 + nu) * (1 - 2 * nu)); }
+double lame_mu(double E, double nu) { return E / (2 * (1 + nu)); }
+double bulk_K(double E, double nu) { return E / (3 * (1 - 2 * nu)); }
+
+std::string ccoord_str(const int *res, int dim, long long idx) {
+  int c[3] = {0, 0, 0};
+  for (int d = dim - 1; d >= 0; --d) {
+    c[d] = (int)(idx % res[d]);
+    idx /= res[d];
+  }
+  std::ostringstream o;
+  o << "(";
+  for (int d = 0; d < dim; ++d) o << (d ? ", " : "") << c[d];
+  o << ")";
+  return o.str();
+}
+
+struct Material {
+  int law = 0;
+  std::string name;
+  double E = 0, nu = 0, tau_y0 = 0, H = 0;
+  int logm_mode = 0;
+  std::vector<long long> pixels;
+  std::vector<double> per_pixel;  // stride values per pixel
+  int stride = 0;
+};
+
+}  // namespace
+
+struct musg_cell {
+  int dim = 0, form = 0, flags = 0;
+  int res[3] = {1, 1, 1};
+  double lengths[3] = {1, 1, 1};
+  long long npx = 0;
+  int D2 = 0;
+  bool initialised = false;
+  bool tangent_valid = false;
+  bool need32 = false;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  std::vector<Material> materials;
+  Spectral sp;
+  int tkind = TK_SMALL;
+  int hep_cur = 0;
+  bool has_le2 = false, has_hep = false;
+  // device fields (FP64 component planes)
+  DevBuf F, P, rhs, io, io2;
+  DevBuf mat, params, law_kind;
+  DevBuf lam64, mu64, lam32, mu32, eig;
+  DevBuf Fprev[2], be[2], eps[2];
+  DevBuf S64, S32, Kp64, Kp32, Fc64, Fc32, Kfull;
+  DevBuf partial, scal;  // reduction scratch, small device scalars
+  DevBuf nonfinite;
+  double *hscal = nullptr;  // pinned host mirror of scal
+
+  ~musg_cell() {
+    if (hscal) cudaFreeHost(hscal);
+    sp.release();
+    if (own_stream && stream) cudaStreamDestroy(stream);
+  }
+  long long nb_dof() const { return npx * D2; }
+  size_t plane_bytes() const { return (size_t)npx * sizeof(double); }
+  size_t field_bytes() const { return (size_t)nb_dof() * sizeof(double); }
+
+  void create(int dim_, const int *res_, const double *len_, int form_, int flags_) {
+    require(dim_ == 2 || dim_ == 3, MUSG_ERR_ARGUMENT, "only 2- and 3-dimensional cells are supported");
+    require(form_ == MUSG_FINITE_STRAIN || form_ == MUSG_SMALL_STRAIN, MUSG_ERR_ARGUMENT, "unknow formulation");
+    dim = dim_;
+    form = form_;
+    flags = flags_;
+    npx = 1;
+    for (int d = 0; d < dim; ++d) {
+      require(res_[d] > 0, MUSG_ERR_ARGUMENT, "resolutions must be positive");
+      res[d] = res_[d];
+      lengths[d] = len_ ? len_[d] : 1.0;
+      npx *= res[d];
+    }
+    D2 = dim * dim;
+    // projections reject even grids (projection_small_strain.cc:46-51,
+    // projection_finite_strain_fast.cc:50-55) unless the extension is asked for
+    if (!(flags & MUSG_FLAG_ALLOW_EVEN))
+      for (int d = 0; d < dim; ++d)
+        require(res[d] % 2 == 1, MUSG_ERR_PROJECTION, "Only an odd number of gridpoints in each direction is supported");
+    MUSG_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+    own_stream = true;
+    const int proj = form == MUSG_FINITE_STRAIN ? MUSG_PROJ_FINITE_STRAIN_FAST : MUSG_PROJ_SMALL_STRAIN;
+    sp.init(dim, res, D2, proj, lengths, (flags & MUSG_FLAG_ALLOW_EVEN) != 0, false);
+    F.alloc(field_bytes());
+    P.alloc(field_bytes());
+    rhs.alloc(field_bytes());
+    MUSG_CUDA(cudaMemsetAsync(F.p, 0, field_bytes(), stream));
+    MUSG_CUDA(cudaMemsetAsync(P.p, 0, field_bytes(), stream));
+    partial.alloc((size_t)std::max<long long>(4 * 4096, 2 * sp.g.nrows + 64) * sizeof(double));
+    scal.alloc(64 * sizeof(double));
+    nonfinite.alloc(sizeof(int));
+    MUSG_CUDA(cudaMemsetAsync(nonfinite.p, 0, sizeof(int), stream));
+    MUSG_CUDA(cudaMallocHost(&hscal, 64 * sizeof(double)));
+    MUSG_CUDA(cudaStreamSynchronize(stream));
+  }
+
+  // device vector of D2 doubles (column-major matrix) into scal[off..]
+  double *put_matrix(const double *m, int off) {
+    for (int c = 0; c < D2; ++c) hscal[off + c] = m[c];
+    MUSG_CUDA(cudaMemcpyAsync(scal.as<double>() + off, hscal + off, D2 * sizeof(double), cudaMemcpyHostToDevice, stream));
+    MUSG_CUDA(cudaStreamSynchronize(stream));  // the pinned slot may be rewritten next
+    return scal.as<double>() + off;
+  }
+
+  void check_material_coverage() {
+    // cell_base.cc:486-526
+    std::vector<int> owner(npx, -1);
+    for (size_t m = 0; m < materials.size(); ++m)
+      for (long long p : materials[m].pixels) {
+        if (owner[p] != -1) {
+          std::ostringstream e;
+          e << "Pixel " << ccoord_str(res, dim, p) << "is already assigned to material '" << materials[owner[p]].name
+            << "' and cannot be reassigned to material '" << materials[m].name;
+          throw Error(MUSG_ERR_RUNTIME, e.str());
+        }
+        owner[p] = (int)m;
+      }
+    long long missing = 0;
+    std::ostringstream e;
+    e << "The following pixels have were not assigned a material: ";
+    for (long long p = 0; p < npx; ++p)
+      if (owner[p] < 0) {
+        if (missing < 16) e << ccoord_str(res, dim, p) << ", ";
+        ++missing;
+      }
+    if (missing) {
+      if (missing > 16) e << "... (" << missing << " pixels), ";
+      e << "and that cannot be handled";
+      throw Error(MUSG_ERR_RUNTIME, e.str());
+    }
+  }
+
+  void initialise() {
+    if (initialised) return;
+    require(!materials.empty(), MUSG_ERR_RUNTIME, "no materials in the cell");
+    require(materials.size() <= (size_t)kMaxMaterials, MUSG_ERR_ARGUMENT, "at most 256 materials per cell");
+    check_material_coverage();
+    std::vector<uint8_t> hmat(npx);
+    std::vector<double> hlam(npx), hmu(npx);
+    std::vector<MatParams> hp(materials.size());
+    std::vector<uint8_t> hkind(kMaxMaterials, TK_FINITE);
+    bool any_le = false;
+    for (size_t m = 0; m < materials.size(); ++m) {
+      const Material &mt = materials[m];
+      MatParams &q = hp[m];
+      q.law = mt.law;
+      q.logm_mode = mt.logm_mode;
+      q.lam = lame_lambda(mt.E, mt.nu);
+      q.mu = lame_mu(mt.E, mt.nu);
+      q.K = bulk_K(mt.E, mt.nu);
+      q.tau_y0 = mt.tau_y0;
+      q.H = mt.H;
+      if (mt.law == MUSG_LAW_HEP1) {
+        has_hep = true;
+        hkind[m] = TK_KPRIME;
+      } else {
+        any_le = true;
+      }
+      if (mt.law == MUSG_LAW_LE2) has_le2 = true;
+      for (size_t k = 0; k < mt.pixels.size(); ++k) {
+        const long long p = mt.pixels[k];
+        hmat[p] = (uint8_t)m;
+        if (mt.law == MUSG_LAW_LE3 || mt.law == MUSG_LAW_LE4) {
+          const double E = mt.per_pixel[2 * k], nu = mt.per_pixel[2 * k + 1];
+          hlam[p] = lame_lambda(E, nu);
+          hmu[p] = lame_mu(E, nu);
+        } else {
+          hlam[p] = q.lam;
+          hmu[p] = q.mu;
+        }
+      }
+    }
+    require(!(has_hep && form == MUSG_SMALL_STRAIN), MUSG_ERR_ARGUMENT,
+            "MaterialHyperElastoPlastic1 needs the finite-strain formulation");
+    if (form == MUSG_SMALL_STRAIN) tkind = TK_SMALL;
+    else if (has_hep && any_le) tkind = TK_MIXED;
+    else if (has_hep) tkind = TK_KPRIME;
+    else tkind = TK_FINITE;
+    mat.alloc(npx);
+    MUSG_CUDA(cudaMemcpy(mat.p, hmat.data(), npx, cudaMemcpyHostToDevice));
+    params.alloc(hp.size() * sizeof(MatParams));
+    MUSG_CUDA(cudaMemcpy(params.p, hp.data(), hp.size() * sizeof(MatParams), cudaMemcpyHostToDevice));
+    law_kind.alloc(kMaxMaterials);
+    MUSG_CUDA(cudaMemcpy(law_kind.p, hkind.data(), kMaxMaterials, cudaMemcpyHostToDevice));
+    lam64.alloc(plane_bytes());
+    mu64.alloc(plane_bytes());
+    MUSG_CUDA(cudaMemcpy(lam64.p, hlam.data(), plane_bytes(), cudaMemcpyHostToDevice));
+    MUSG_CUDA(cudaMemcpy(mu64.p, hmu.data(), plane_bytes(), cudaMemcpyHostToDevice));
+    if (has_le2) {
+      std::vector<double> h((size_t)npx * D2, 0.0);
+      for (const Material &mt : materials)
+        if (mt.law == MUSG_LAW_LE2)
+          for (size_t k = 0; k < mt.pixels.size(); ++k)
+            for (int c = 0; c < D2; ++c) h[(size_t)c * npx + mt.pixels[k]] = mt.per_pixel[k * D2 + c];
+      eig.alloc(field_bytes());
+      MUSG_CUDA(cudaMemcpy(eig.p, h.data(), field_bytes(), cudaMemcpyHostToDevice));
+    }
+    if (form == MUSG_FINITE_STRAIN) {
+      S64.alloc(field_bytes());
+      Fc64.alloc(field_bytes());  // F at the last evaluation (the tangent's F)
+    }
+    if (has_hep) {
+      // material_hyper_elasto_plastic1.cc:76-84: zero-initialised state fields,
+      // current() of F_prev and b_e set to I, then one cycle
+      for (int b = 0; b < 2; ++b) {
+        Fprev[b].alloc(field_bytes());
+        be[b].alloc(field_bytes());
+        eps[b].alloc(plane_bytes());
+        MUSG_CUDA(cudaMemset(Fprev[b].p, 0, field_bytes()));
+        MUSG_CUDA(cudaMemset(be[b].p, 0, field_bytes()));
+        MUSG_CUDA(cudaMemset(eps[b].p, 0, plane_bytes()));
+      }
+      std::vector<double> I(D2, 0.0);
+      for (int i = 0; i < dim; ++i) I[i + dim * i] = 1.0;
+      double *Id = put_matrix(I.data(), 0);
+      fill_uniform(Fprev[0].as<double>(), Id, D2, npx, stream);
+      fill_uniform(be[0].as<double>(), Id, D2, npx, stream);
+      hep_cur = 1;
+      Kp64.alloc((size_t)npx * D2 * dim * sizeof(double));
+    }
+    if (need32) alloc32();
+    MUSG_CUDA(cudaStreamSynchronize(stream));
+    initialised = true;
+  }
+
+  void alloc32() {
+    need32 = true;
+    sp.ensure32();
+    if (!initialised && !lam64.p) return;  // done at initialise
+    if (!lam32.p) {
+      lam32.alloc((size_t)npx * sizeof(float));
+      mu32.alloc((size_t)npx * sizeof(float));
+      convert<float, double>(lam32.as<float>(), lam64.as<double>(), npx, 1.0, stream);
+      convert<float, double>(mu32.as<float>(), mu64.as<double>(), npx, 1.0, stream);
+    }
+    if (form == MUSG_FINITE_STRAIN) {
+      if (!S32.p) S32.alloc((size_t)nb_dof() * sizeof(float));
+      if (!Fc32.p) Fc32.alloc((size_t)nb_dof() * sizeof(float));
+      if (has_hep && !Kp32.p) Kp32.alloc((size_t)npx * D2 * dim * sizeof(float));
+    }
+    tangent_valid = false;
+  }
+
+  void evaluate(bool want_K) {
+    if (!initialised) initialise();
+    MaterialArgs a{};
+    a.dim = dim;
+    a.form = form;
+    a.npx = npx;
+    a.F = F.as<double>();
+    a.P = P.as<double>();
+    a.mat = mat.as<uint8_t>();
+    a.params = params.as<MatParams>();
+    a.lam = lam64.as<double>();
+    a.mu = mu64.as<double>();
+    a.eig = has_le2 ? eig.as<double>() : nullptr;
+    for (int b = 0; b < 2; ++b) {
+      a.Fprev[b] = Fprev[b].as<double>();
+      a.be[b] = be[b].as<double>();
+      a.eps[b] = eps[b].as<double>();
+    }
+    a.cur = hep_cur;
+    a.S64 = S64.as<double>();
+    a.Kp64 = Kp64.as<double>();
+    a.S32 = S32.as<float>();
+    a.Kp32 = Kp32.as<float>();
+    a.Fc32 = Fc32.as<float>();
+    a.Fc64 = Fc64.as<double>();
+    if (want_K) {
+      if (Kfull.bytes < (size_t)nb_dof() * D2 * sizeof(double)) Kfull.alloc((size_t)nb_dof() * D2 * sizeof(double));
+      a.Kfull = Kfull.as<double>();
+    }
+    a.nonfinite = nonfinite.as<int>();
+    material_evaluate(a, stream);
+    tangent_valid = true;
+  }
+
+  template <typename R> TangentData<R> tangent() const;
+
+  void save_history() {
+    // StateField::cycle (statefield.hh:322-326): swap current and old
+    if (has_hep) hep_cur = 1 - hep_cur;
+  }
+
+  // host AoS vector -> device SoA planes (dst)
+  void upload_field(const double *host, double *dst) {
+    if (io.bytes < field_bytes()) io.alloc(field_bytes());
+    MUSG_CUDA(cudaMemcpyAsync(io.p, host, field_bytes(), cudaMemcpyHostToDevice, stream));
+    aos_to_soa(io.as<double>(), dst, D2, npx, stream);
+  }
+  void download_field(const double *src, double *host) {
+    if (io.bytes < field_bytes()) io.alloc(field_bytes());
+    soa_to_aos(src, io.as<double>(), D2, npx, stream);
+    MUSG_CUDA(cudaMemcpyAsync(host, io.p, field_bytes(), cudaMemcpyDeviceToHost, stream));
+    MUSG_CUDA(cudaStreamSynchronize(stream));
+  }
+};
+
+template <> TangentData<double> musg_cell::tangent<double>() const {
+  TangentData<double> t;
+  t.lam = lam64.as<double>();
+  t.mu = mu64.as<double>();
+  t.F = Fc64.as<double>();
+  t.S = S64.as<double>();
+  t.Kp = Kp64.as<double>();
+  t.mat = mat.as<uint8_t>();
+  t.law_kind = law_kind.as<uint8_t>();
+  return t;
+}
+
+template <> TangentData<float> musg_cell::tangent<float>() const {
+  TangentData<float> t;
+  t.lam = lam32.as<float>();
+  t.mu = mu32.as<float>();
+  t.F = Fc32.as<float>();
+  t.S = S32.as<float>();
+  t.Kp = Kp32.as<float>();
+  t.mat = mat.as<uint8_t>();
+  t.law_kind = law_kind.as<uint8_t>();
+  return t;
+}
+
+// ---------------------------------------------------------------------- solver
+struct musg_solver {
+  musg_cell *cell = nullptr;
+  double tol = 0;
+  unsigned maxiter = 0;
+  int verbose = 0;
+  int precision = MUSG_PRECISION_FP64;
+  bool converged = false;
+  unsigned long long counter = 0;
+  DevBuf x, r, p, Ap, st;
+  CGState *hst = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  unsigned long long graph_nodes = 0;
+  int chunk = 16;
+  bool graphs = true;
+  // mixed precision: the FP32 inner solve stops at max(tol, inner_tol); FP32 CG
+  // cannot reach residuals much below ~1e-6 on stiff-contrast cells and diverges
+  // past that point, so the FP64 Newton loop refines instead
+  double inner_tol = 1e-5;
+
+  ~musg_solver() {
+    if (exec) cudaGraphExecDestroy(exec);
+    if (hst) cudaFreeHost(hst);
+  }
+
+  size_t rbytes() const { return precision == MUSG_PRECISION_MIXED ? sizeof(float) : sizeof(double); }
+
+  void create(musg_cell *c, double tol_, unsigned maxiter_, int verbose_, int precision_) {
+    require(c != nullptr, MUSG_ERR_ARGUMENT, "null cell");
+    require(precision_ == MUSG_PRECISION_FP64 || precision_ == MUSG_PRECISION_MIXED, MUSG_ERR_ARGUMENT,
+            "unknown precision");
+    cell = c;
+    tol = tol_;
+    maxiter = maxiter_;
+    verbose = verbose_;
+    precision = precision_;
+    if (precision == MUSG_PRECISION_MIXED) cell->alloc32();
+    const size_t n = (size_t)cell->nb_dof();
+    x.alloc(n * rbytes());
+    r.alloc(n * rbytes());
+    p.alloc(n * rbytes());
+    Ap.alloc(n * rbytes());
+    st.alloc(sizeof(CGState));
+    MUSG_CUDA(cudaMemset(st.p, 0, sizeof(CGState)));
+    MUSG_CUDA(cudaMallocHost(&hst, sizeof(CGState)));
+    memset(hst, 0, sizeof(CGState));
+    const char *env = getenv("MUSG_CG_GRAPHS");
+    if (env && env[0] == '0') graphs = false;
+    if (verbose) chunk = 1;
+  }
+
+  // one CG iteration (solver_cg.cc:76-97); ev, when given, receives an event
+  // before the first and after every kernel (profiling)
+  template <typename R> int iteration(cudaStream_t s, cudaEvent_t *ev = nullptr) {
+    musg_cell &c = *cell;
+    const long long n = c.nb_dof();
+    CGState *d = st.as<CGState>();
+    double *part = c.partial.as<double>();
+    const TangentData<R> td = c.tangent<R>();
+    const int nop = cg_operator<R>(c.sp, c.tkind, td, d, r.as<R>(), p.as<R>(), Ap.as<R>(), part, s, ev);
+    int k = c.dim == 3 ? 5 : 3;
+    cg_finalize_alpha(d, part, nop, s);
+    if (ev) MUSG_CUDA(cudaEventRecord(ev[++k], s));
+    cg_update<R>(d, x.as<R>(), r.as<R>(), p.as<R>(), Ap.as<R>(), n, part, s);
+    if (ev) MUSG_CUDA(cudaEventRecord(ev[++k], s));
+    cg_finalize_beta(d, part, reduce_blocks(n), s);
+    if (ev) MUSG_CUDA(cudaEventRecord(ev[++k], s));
+    return k;  // number of kernels
+  }
+
+  static const char *kernel_name(int dim, int k) {
+    static const char *n3[] = {"last_axis_fwd_tangent", "axis1_fwd", "green_axis0", "axis1_inv", "last_axis_inv_dot",
+                               "cg_alpha", "cg_update", "cg_beta"};
+    static const char *n2[] = {"last_axis_fwd_tangent", "green_axis0", "last_axis_inv_dot", "cg_alpha", "cg_update",
+                               "cg_beta"};
+    if (dim == 3) return (k >= 0 && k < 8) ? n3[k] : "";
+    return (k >= 0 && k < 6) ? n2[k] : "";
+  }
+
+  // mean per-kernel durations (ms) over `iters` eagerly launched iterations started
+  // from the cell's last residual, timed with CUDA events on the cell's stream
+  template <typename R> int profile(int iters, double *ms) {
+    musg_cell &c = *cell;
+    cudaStream_t s = c.stream;
+    require(c.tangent_valid, MUSG_ERR_RUNTIME, "profile needs an evaluated tangent");
+    const long long n = c.nb_dof();
+    double *part = c.partial.as<double>();
+    cg_init<R>(st.as<CGState>(), c.rhs.as<double>(), r.as<R>(), x.as<R>(), n, 0.0, iters, part, part + 4096, s);
+    const int nk = c.dim == 3 ? 8 : 6;
+    std::vector<cudaEvent_t> ev(nk + 1);
+    for (auto &e : ev) MUSG_CUDA(cudaEventCreate(&e));
+    std::vector<double> acc(nk, 0.0);
+    for (int it = 0; it < iters; ++it) {
+      iteration<R>(s, ev.data());
+      MUSG_CUDA(cudaEventSynchronize(ev[nk]));
+      for (int k = 0; k < nk; ++k) {
+        float t = 0;
+        MUSG_CUDA(cudaEventElapsedTime(&t, ev[k], ev[k + 1]));
+        acc[k] += t;
+      }
+    }
+    for (auto &e : ev) cudaEventDestroy(e);
+    for (int k = 0; k < nk; ++k) ms[k] = acc[k] / std::max(iters, 1);
+    // leave the solver as after a finished solve (counter untouched by profiling)
+    MUSG_CUDA(cudaMemcpyAsync(hst, st.p, sizeof(CGState), cudaMemcpyDeviceToHost, s));
+    MUSG_CUDA(cudaStreamSynchronize(s));
+    hst->counter = counter;
+    MUSG_CUDA(cudaMemcpyAsync(st.p, hst, sizeof(CGState), cudaMemcpyHostToDevice, s));
+    MUSG_CUDA(cudaStreamSynchronize(s));
+    return nk;
+  }
+
+  template <typename R> void build_graph() {
+    if (exec) return;
+    cudaStream_t s = cell->stream;
+    cudaGraph_t g = nullptr;
+    const unsigned long long before = g_launches.load();
+    MUSG_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeRelaxed));
+    try {
+      for (int k = 0; k < chunk; ++k) iteration<R>(s);
+    } catch (...) {
+      cudaStreamEndCapture(s, &g);
+      if (g) cudaGraphDestroy(g);
+      throw;
+    }
+    MUSG_CUDA(cudaStreamEndCapture(s, &g));
+    // captured launches did not run; replays account for them
+    graph_nodes = g_launches.load() - before;
+    g_launches.fetch_sub(graph_nodes);
+    MUSG_CUDA(cudaGraphInstantiate(&exec, g, 0));
+    cudaGraphDestroy(g);
+  }
+
+  // SolverCG::solve (solver_cg.cc:54-110) on a device rhs (FP64 SoA planes)
+  template <typename R> void solve_device(const double *rhs) {
+    musg_cell &c = *cell;
+    cudaStream_t s = c.stream;
+    const long long n = c.nb_dof();
+    double *part = c.partial.as<double>();
+    // r = A 0 - rhs = -rhs, p = -r (first iteration), x = 0
+    const double t = (precision == MUSG_PRECISION_MIXED) ? std::max(tol, inner_tol) : tol;
+    cg_init<R>(st.as<CGState>(), rhs, r.as<R>(), x.as<R>(), n, t, (int)maxiter, part, part + 4096, s);
+    converged = false;
+    if (graphs && !verbose) build_graph<R>();
+    for (;;) {
+      if (exec) {
+        MUSG_CUDA(cudaGraphLaunch(exec, s));
+        g_launches.fetch_add(graph_nodes);
+      } else {
+        for (int k = 0; k < chunk; ++k) iteration<R>(s);
+      }
+      MUSG_CUDA(cudaMemcpyAsync(hst, st.p, sizeof(CGState), cudaMemcpyDeviceToHost, s));
+      MUSG_CUDA(cudaStreamSynchronize(s));
+      if (verbose) {
+        printf("  at CG step %d: |r|/|b| = %15g, cg_tol = %g\n", hst->iter - 1,
+               std::sqrt(hst->rdr / hst->rhs_norm2), tol);
+        fflush(stdout);
+      }
+      if (!hst->active) break;
+    }
+    counter = hst->counter;
+    if (hst->rdr < hst->tol2) {
+      converged = true;
+    } else {
+      std::ostringstream e;
+      e << "Conjugate gradient has not converged. After " << counter << " steps, the solver  FAILED with  |r|/|b| = "
+        << std::sqrt(hst->rdr / hst->rhs_norm2) << ", cg_tol = " << std::sqrt(hst->tol2 / hst->rhs_norm2);
+      throw Error(MUSG_ERR_CONVERGENCE, e.str());
+    }
+  }
+
+  void solve_device_any(const double *rhs) {
+    if (precision == MUSG_PRECISION_MIXED) solve_device<float>(rhs);
+    else solve_device<double>(rhs);
+  }
+
+  void reset_counter() {
+    counter = 0;
+    MUSG_CUDA(cudaMemsetAsync(&st.as<CGState>()->counter, 0, sizeof(unsigned long long), cell->stream));
+    MUSG_CUDA(cudaStreamSynchronize(cell->stream));
+  }
+};
+
+// ---------------------------------------------------------------------- FFT / projection handles
+struct musg_fft {
+  Spectral sp;
+  cudaStream_t stream = nullptr;
+  DevBuf a, b;
+  ~musg_fft() {
+    sp.release();
+    if (stream) cudaStreamDestroy(stream);
+  }
+};
+
+struct musg_projection {
+  Spectral sp;
+  int kind = 0;
+  cudaStream_t stream = nullptr;
+  DevBuf a, b;
+  ~musg_projection() {
+    sp.release();
+    if (stream) cudaStreamDestroy(stream);
+  }
+};
+
+// ---------------------------------------------------------------------- newton_cg
+namespace {
+
+void check_symmetry_or_throw(const double *m, int dim) {
+  // solver_common.cc:39-43 with rel_tol = 1e-8
+  double n = 0, a = 0;
+  for (int j = 0; j < dim; ++j)
+    for (int i = 0; i < dim; ++i) {
+      n += m[i + dim * j] * m[i + dim * j];
+      const double d = m[i + dim * j] - m[j + dim * i];
+      a += d * d;
+    }
+  n = std::sqrt(n);
+  a = std::sqrt(a);
+  const double rel = 1e-8;
+  if (!(rel >= a / n || rel >= n)) throw Error(MUSG_ERR_SOLVER, "all Δε must be symmetric!");
+}
+
+void newton_cg_impl(musg_cell *cell, const double *steps, int nsteps, musg_solver *solver, double newton_tol,
+                    double equil_tol, int verbose, musg_result_info *infos, double *grads, double *stresses) {
+  require(cell && solver && steps && nsteps > 0, MUSG_ERR_ARGUMENT, "invalid newton_cg arguments");
+  require(solver->cell == cell, MUSG_ERR_ARGUMENT, "solver belongs to another cell");
+  musg_cell &c = *cell;
+  const int dim = c.dim, D2 = c.D2;
+  cudaStream_t s = c.stream;
+  if (!c.initialised) c.initialise();
+  // solvers.cc:98-131: uniform initial strain, load-step checks
+  std::vector<double> I(D2, 0.0);
+  if (c.form == MUSG_FINITE_STRAIN)
+    for (int i = 0; i < dim; ++i) I[i + dim * i] = 1.0;
+  else
+    for (int k = 0; k < nsteps; ++k) check_symmetry_or_throw(steps + (size_t)k * D2, dim);
+  fill_uniform(c.F.as<double>(), c.put_matrix(I.data(), 0), D2, c.npx, s);
+  if (verbose > 0) {
+    printf("Newton-CG for %s strain with\nnewton_tol = %g, cg_tol = %g maxiter = %u\n",
+           c.form == MUSG_FINITE_STRAIN ? "finite" : "small", newton_tol, solver->tol, solver->maxiter);
+  }
+  std::vector<double> previous(D2, 0.0);
+  const long long n = c.nb_dof();
+  double *dscal = c.scal.as<double>();
+  for (int step = 0; step < nsteps; ++step) {
+    const double *macro = steps + (size_t)step * D2;
+    std::vector<double> delta(D2);
+    for (int k = 0; k < D2; ++k) delta[k] = macro[k] - previous[k];
+    add_macro(c.F.as<double>(), c.put_matrix(delta.data(), 16), D2, c.npx, s);
+    std::string message = "Has not converged";
+    double incr_norm = 2 * newton_tol, grad_norm = 1, stress_norm = 2 * equil_tol;
+    bool has_converged = false;
+    auto convergence_test = [&]() {
+      const bool incr_test = incr_norm / grad_norm <= newton_tol;
+      const bool stress_test = stress_norm < equil_tol;
+      if (incr_test) message = "Residual  tolerance reached";
+      else if (stress_test) message = "Reached stress divergence tolerance";
+      has_converged = incr_test || stress_test;
+      return has_converged;
+    };
+    unsigned newt_iter = 0;
+    for (; newt_iter < solver->maxiter && !has_converged; ++newt_iter) {
+      c.evaluate(false);
+      // rhs = -P, projected (FP64)
+      spectral_project<double>(c.sp, c.P.as<double>(), c.rhs.as<double>(), -1.0, s);
+      dot_device<double, double>(c.rhs.as<double>(), c.rhs.as<double>(), n, c.partial.as<double>(), dscal + 32, s);
+      MUSG_CUDA(cudaMemcpyAsync(c.hscal + 32, dscal + 32, sizeof(double), cudaMemcpyDeviceToHost, s));
+      MUSG_CUDA(cudaStreamSynchronize(s));
+      stress_norm = std::sqrt(c.hscal[32]);
+      if (convergence_test()) break;
+      solver->solve_device_any(c.rhs.as<double>());
+      if (solver->precision == MUSG_PRECISION_MIXED)
+        newton_update<float>(c.F.as<double>(), solver->x.as<float>(), n, c.partial.as<double>(), dscal + 34, s);
+      else
+        newton_update<double>(c.F.as<double>(), solver->x.as<double>(), n, c.partial.as<double>(), dscal + 34, s);
+      MUSG_CUDA(cudaMemcpyAsync(c.hscal + 34, dscal + 34, 2 * sizeof(double), cudaMemcpyDeviceToHost, s));
+      MUSG_CUDA(cudaStreamSynchronize(s));
+      incr_norm = std::sqrt(c.hscal[34]);
+      grad_norm = std::sqrt(c.hscal[35]);
+      if (verbose > 0) {
+        printf("at Newton step %u, |δ%s|/|Δ%s| = %17g, tol = %g\n", newt_iter, c.form == MUSG_FINITE_STRAIN ? "F" : "ε",
+               c.form == MUSG_FINITE_STRAIN ? "F" : "ε", incr_norm / grad_norm, newton_tol);
+        fflush(stdout);
+      }
+      convergence_test();
+    }
+    previous.assign(macro, macro + D2);
+    // mixed precision: the stress of the last evaluation carries the FP32 inner
+    // tolerance, so history-free cells return P at the final strain instead
+    if (solver->precision == MUSG_PRECISION_MIXED && !c.has_hep) c.evaluate(false);
+    const bool conv = convergence_test();
+    if (infos) {
+      musg_result_info &ri = infos[step];
+      ri.success = conv ? 1 : 0;
+      ri.status = conv ? 1 : 0;
+      ri.nb_it = newt_iter;
+      ri.nb_fev = (unsigned)solver->counter;
+      memset(ri.message, 0, sizeof(ri.message));
+      strncpy(ri.message, message.c_str(), sizeof(ri.message) - 1);
+    }
+    if (grads) c.download_field(c.F.as<double>(), grads + (size_t)step * n);
+    if (stresses) c.download_field(c.P.as<double>(), stresses + (size_t)step * n);
+    c.save_history();
+  }
+  MUSG_CUDA(cudaStreamSynchronize(s));
+}
+
+}  // namespace
+
+// ====================================================================== C ABI
+extern "C" {
+
+const char *musg_last_error(void) { return g_last_error.c_str(); }
+
+int musg_version(void) { return 100; }
+
+int musg_set_device(int device) {
+  return guard([&] { MUSG_CUDA(cudaSetDevice(device)); });
+}
+
+int musg_device_count(int *count) {
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess) {
+    cudaGetLastError();
+    n = 0;
+  }
+  if (count) *count = n;
+  return MUSG_OK;
+}
+
+int musg_cell_create(int dim, const int *resolutions, const double *lengths, int formulation, int flags,
+                     musg_cell **out) {
+  return guard([&] {
+    require(out && resolutions, MUSG_ERR_ARGUMENT, "null argument");
+    auto c = std::make_unique<musg_cell>();
+    c->create(dim, resolutions, lengths, formulation, flags);
+    *out = c.release();
+  });
+}
+
+int musg_cell_destroy(musg_cell *cell) {
+  return guard([&] { delete cell; });
+}
+
+int musg_cell_sizes(musg_cell *cell, long long *nb_dof, long long *nb_pixels) {
+  return guard([&] {
+    require(cell, MUSG_ERR_ARGUMENT, "null cell");
+    if (nb_dof) *nb_dof = cell->nb_dof();
+    if (nb_pixels) *nb_pixels = cell->npx;
+  });
+}
+
+int musg_cell_set_stream(musg_cell *cell, void *cuda_stream) {
+  return guard([&] {
+    require(cell, MUSG_ERR_ARGUMENT, "null cell");
+    MUSG_CUDA(cudaStreamSynchronize(cell->stream));
+    if (cell->own_stream) cudaStreamDestroy(cell->stream);
+    cell->own_stream = false;
+    cell->stream = (cudaStream_t)cuda_stream;
+  });
+}
+
+int musg_material_create(musg_cell *cell, int law, const char *name, const double *params, int nb_params,
+                         int *material) {
+  return guard([&] {
+    require(cell, MUSG_ERR_ARGUMENT, "null cell");
+    require(!cell->initialised, MUSG_ERR_RUNTIME, "cannot add materials to an initialised cell");
+    Material m;
+    m.law = law;
+    m.name = name ? name : "";
+    switch (law) {
+      case MUSG_LAW_LE1:
+      case MUSG_LAW_LE2:
+        require(nb_params >= 2, MUSG_ERR_ARGUMENT, "this material needs (Young, Poisson)");
+        m.E = params[0];
+        m.nu = params[1];
+        m.stride = law == MUSG_LAW_LE2 ? cell->D2 : 0;
+        break;
+      case MUSG_LAW_LE3:
+      case MUSG_LAW_LE4:
+        m.stride = 2;
+        break;
+      case MUSG_LAW_HEP1:
+        require(nb_params >= 4, MUSG_ERR_ARGUMENT, "this material needs (Young, Poisson, tau_y0, H)");
+        m.E = params[0];
+        m.nu = params[1];
+        m.tau_y0 = params[2];
+        m.H = params[3];
+        m.logm_mode = nb_params >= 5 ? (int)params[4] : 0;
+        break;
+      default:
+        throw Error(MUSG_ERR_ARGUMENT, "unknown material law");
+    }
+    cell->materials.push_back(std::move(m));
+    if (material) *material = (int)cell->materials.size() - 1;
+  });
+}
+
+int musg_material_add_pixels(musg_cell *cell, int material, const long long *pixels, long long count,
+                             const double *per_pixel, int stride) {
+  return guard([&] {
+    require(cell, MUSG_ERR_ARGUMENT, "null cell");
+    require(!cell->initialised, MUSG_ERR_RUNTIME, "cannot add pixels to an initialised cell");
+    require(material >= 0 && material < (int)cell->materials.size(), MUSG_ERR_ARGUMENT, "unknown material");
+    Material &m = cell->materials[material];
+    if (m.stride > 0) {
+      if (m.law == MUSG_LAW_LE2)
+        require(per_pixel && stride == m.stride, MUSG_ERR_RUNTIME, "this material needs pixels with and eigenstrain");
+      else
+        require(per_pixel && stride == m.stride, MUSG_ERR_RUNTIME,
+                "this material needs pixels with Youngs modulus and Poisson ratio.");
+    }
+    for (long long k = 0; k < count; ++k) {
+      require(pixels[k] >= 0 && pixels[k] < cell->npx, MUSG_ERR_ARGUMENT, "pixel index out of range");
+      m.pixels.push_back(pixels[k]);
+      for (int s = 0; s < m.stride; ++s) m.per_pixel.push_back(per_pixel[k * stride + s]);
+    }
+  });
+}
+
+int musg_material_size(musg_cell *cell, int material, long long *count) {
+  return guard([&] {
+    require(cell && material >= 0 && material < (int)cell->materials.size(), MUSG_ERR_ARGUMENT, "unknown material");
+    *count = (long long)cell->materials[material].pixels.size();
+  });
+}
+
+int musg_cell_initialise(musg_cell *cell, int plan_flags) {
+  return guard([&] {
+    require(cell, MUSG_ERR_ARGUMENT, "null cell");
+    require(plan_flags >= 0 && plan_flags <= 2, MUSG_ERR_ARGUMENT, "unknown planner flag type");
+    cell->initialise();
+  });
+}
+
+int musg_cell_set_uniform_strain(musg_cell *cell, const double *strain) {
+  return guard([&] {
+    require(cell && strain, MUSG_ERR_ARGUMENT, "null argument");
+    fill_uniform(cell->F.as<double>(), cell->put_matrix(strain, 0), cell->D2, cell->npx, cell->stream);
+    MUSG_CUDA(cudaStreamSynchronize(cell->stream));
+  });
+}
+
+int musg_cell_get_strain(musg_cell *cell, double *out) {
+  return guard([&] {
+    require(cell && out, MUSG_ERR_ARGUMENT, "null argument");
+    if (!cell->initialised) cell->initialise();  // CellBase::get_strain initialises
+    cell->download_field(cell->F.as<double>(), out);
+  });
+}
+
+int musg_cell_set_strain(musg_cell *cell, const double *in) {
+  return guard([&] {
+    require(cell && in, MUSG_ERR_ARGUMENT, "null argument");
+    cell->upload_field(in, cell->F.as<double>());
+    MUSG_CUDA(cudaStreamSynchronize(cell->stream));
+  });
+}
+
+int musg_cell_get_stress(musg_cell *cell, double *out) {
+  return guard([&] {
+    require(cell && out, MUSG_ERR_ARGUMENT, "null argument");
+    cell->download_field(cell->P.as<double>(), out);
+  });
+}
+
+int musg_cell_evaluate_stress_tangent(musg_cell *cell, double *stress_out, double *tangent_out) {
+  return guard([&] {
+    require(cell, MUSG_ERR_ARGUMENT, "null cell");
+    cell->evaluate(tangent_out != nullptr);
+    if (stress_out) cell->download_field(cell->P.as<double>(), stress_out);
+    if (tangent_out) {
+      const size_t bytes = (size_t)cell->nb_dof() * cell->D2 * sizeof(double);
+      MUSG_CUDA(cudaMemcpyAsync(tangent_out, cell->Kfull.p, bytes, cudaMemcpyDeviceToHost, cell->stream));
+    }
+    MUSG_CUDA(cudaStreamSynchronize(cell->stream));
+  });
+}
+
+int musg_cell_apply_projection(musg_cell *cell, double *vec) {
+  return guard([&] {
+    require(cell && vec, MUSG_ERR_ARGUMENT, "null argument");
+    musg_cell &c = *cell;
+    if (c.io2.bytes < c.field_bytes()) c.io2.alloc(c.field_bytes());
+    c.upload_field(vec, c.io2.as<double>());
+    spectral_project<double>(c.sp, c.io2.as<double>(), c.io2.as<double>(), 1.0, c.stream);
+    c.download_field(c.io2.as<double>(), vec);
+  });
+}
+
+int musg_cell_directional_stiffness(musg_cell *cell, const double *dF, double *dP) {
+  return guard([&] {
+    require(cell && dF && dP, MUSG_ERR_ARGUMENT, "null argument");
+    musg_cell &c = *cell;
+    require(c.tangent_valid, MUSG_ERR_RUNTIME,
+            "currently only implemented for cases where a stiffness matrix exists");
+    if (c.io2.bytes < c.field_bytes()) c.io2.alloc(c.field_bytes());
+    c.upload_field(dF, c.io2.as<double>());
+    tangent_operator<double>(c.sp, c.tkind, c.tangent<double>(), c.io2.as<double>(), c.io2.as<double>(), c.stream);
+    c.download_field(c.io2.as<double>(), dP);
+  });
+}
+
+int musg_cell_save_history_variables(musg_cell *cell) {
+  return guard([&] {
+    require(cell, MUSG_ERR_ARGUMENT, "null cell");
+    cell->save_history();
+  });
+}
+
+int musg_solver_cg_create(musg_cell *cell, double tol, unsigned maxiter, int verbose, int precision,
+                          musg_solver **out) {
+  return guard([&] {
+    require(out, MUSG_ERR_ARGUMENT, "null argument");
+    auto s = std::make_unique<musg_solver>();
+    s->create(cell, tol, maxiter, verbose, precision);
+    *out = s.release();
+  });
+}
+
+int musg_solver_set_inner_tol(musg_solver *solver, double inner_tol) {
+  return guard([&] {
+    require(solver && inner_tol >= 0, MUSG_ERR_ARGUMENT, "invalid argument");
+    solver->inner_tol = inner_tol;
+  });
+}
+
+int musg_solver_destroy(musg_solver *solver) {
+  return guard([&] { delete solver; });
+}
+
+int musg_solver_get_counter(musg_solver *solver, unsigned *counter) {
+  return guard([&] {
+    require(solver && counter, MUSG_ERR_ARGUMENT, "null argument");
+    *counter = (unsigned)solver->counter;
+  });
+}
+
+int musg_solver_reset_counter(musg_solver *solver) {
+  return guard([&] {
+    require(solver, MUSG_ERR_ARGUMENT, "null solver");
+    solver->reset_counter();
+  });
+}
+
+int musg_solver_has_converged(musg_solver *solver, int *converged) {
+  return guard([&] {
+    require(solver && converged, MUSG_ERR_ARGUMENT, "null argument");
+    *converged = solver->converged ? 1 : 0;
+  });
+}
+
+int musg_solver_solve(musg_solver *solver, const double *rhs, double *x_out) {
+  return guard([&] {
+    require(solver && rhs && x_out, MUSG_ERR_ARGUMENT, "null argument");
+    musg_cell &c = *solver->cell;
+    require(c.tangent_valid, MUSG_ERR_RUNTIME, "currently only implemented for cases where a stiffness matrix exists");
+    if (c.io2.bytes < c.field_bytes()) c.io2.alloc(c.field_bytes());
+    c.upload_field(rhs, c.io2.as<double>());
+    solver->solve_device_any(c.io2.as<double>());
+    if (solver->precision == MUSG_PRECISION_MIXED)
+      convert<double, float>(c.io2.as<double>(), solver->x.as<float>(), c.nb_dof(), 1.0, c.stream);
+    else
+      convert<double, double>(c.io2.as<double>(), solver->x.as<double>(), c.nb_dof(), 1.0, c.stream);
+    c.download_field(c.io2.as<double>(), x_out);
+  });
+}
+
+int musg_launch_count(unsigned long long *count) {
+  return guard([&] {
+    require(count, MUSG_ERR_ARGUMENT, "null argument");
+    *count = g_launches.load();
+  });
+}
+
+int musg_solver_profile(musg_solver *solver, int iterations, double *ms_out, int *nb_kernels) {
+  return guard([&] {
+    require(solver && ms_out && iterations > 0, MUSG_ERR_ARGUMENT, "invalid argument");
+    const int nk = solver->precision == MUSG_PRECISION_MIXED ? solver->profile<float>(iterations, ms_out)
+                                                             : solver->profile<double>(iterations, ms_out);
+    if (nb_kernels) *nb_kernels = nk;
+  });
+}
+
+const char *musg_solver_kernel_name(musg_solver *solver, int k) {
+  if (!solver || !solver->cell) return "";
+  return musg_solver::kernel_name(solver->cell->dim, k);
+}
+
+int musg_newton_cg(musg_cell *cell, const double *load_steps, int nb_steps, musg_solver *solver, double newton_tol,
+                   double equil_tol, int verbose, musg_result_info *infos, double *grads, double *stresses) {
+  return guard([&] {
+    newton_cg_impl(cell, load_steps, nb_steps, solver, newton_tol, equil_tol, verbose, infos, grads, stresses);
+  });
+}
+
+int musg_fft_create(int dim, const int *resolutions, int nb_components, musg_fft **out) {
+  return guard([&] {
+    require(out && resolutions && nb_components > 0, MUSG_ERR_ARGUMENT, "invalid argument");
+    auto f = std::make_unique<musg_fft>();
+    f->sp.init(dim, resolutions, nb_components, -1, nullptr, true, false);
+    MUSG_CUDA(cudaStreamCreateWithFlags(&f->stream, cudaStreamNonBlocking));
+    *out = f.release();
+  });
+}
+
+int musg_fft_destroy(musg_fft *fft) {
+  return guard([&] { delete fft; });
+}
+
+int musg_fft_forward(musg_fft *fft, const double *in, double *out_complex) {
+  return guard([&] {
+    require(fft && in && out_complex, MUSG_ERR_ARGUMENT, "null argument");
+    Spectral &sp = fft->sp;
+    const size_t rb = (size_t)sp.g.npx * sp.ncomp * sizeof(double);
+    const size_t cb = (size_t)sp.g.nk * sp.ncomp * sizeof(double2);
+    if (fft->a.bytes < std::max(rb, cb)) fft->a.alloc(std::max(rb, cb));
+    if (fft->b.bytes < std::max(rb, cb)) fft->b.alloc(std::max(rb, cb));
+    MUSG_CUDA(cudaMemcpyAsync(fft->a.p, in, rb, cudaMemcpyHostToDevice, fft->stream));
+    aos_to_soa(fft->a.as<double>(), fft->b.as<double>(), sp.ncomp, sp.g.npx, fft->stream);
+    spectral_forward<double>(sp, fft->b.as<double>(), 1.0, fft->stream);
+    soa_to_aos_complex((const double2 *)sp.spec64, fft->a.as<double2>(), sp.ncomp, sp.g.nk, fft->stream);
+    MUSG_CUDA(cudaMemcpyAsync(out_complex, fft->a.p, cb, cudaMemcpyDeviceToHost, fft->stream));
+    MUSG_CUDA(cudaStreamSynchronize(fft->stream));
+  });
+}
+
+int musg_fft_inverse(musg_fft *fft, const double *in_complex, double *out) {
+  return guard([&] {
+    require(fft && in_complex && out, MUSG_ERR_ARGUMENT, "null argument");
+    Spectral &sp = fft->sp;
+    const size_t rb = (size_t)sp.g.npx * sp.ncomp * sizeof(double);
+    const size_t cb = (size_t)sp.g.nk * sp.ncomp * sizeof(double2);
+    if (fft->a.bytes < std::max(rb, cb)) fft->a.alloc(std::max(rb, cb));
+    if (fft->b.bytes < std::max(rb, cb)) fft->b.alloc(std::max(rb, cb));
+    MUSG_CUDA(cudaMemcpyAsync(fft->a.p, in_complex, cb, cudaMemcpyHostToDevice, fft->stream));
+    aos_to_soa_complex(fft->a.as<double2>(), (double2 *)sp.spec64, sp.ncomp, sp.g.nk, fft->stream);
+    spectral_inverse<double>(sp, fft->b.as<double>(), 1.0, fft->stream);
+    soa_to_aos(fft->b.as<double>(), fft->a.as<double>(), sp.ncomp, sp.g.npx, fft->stream);
+    MUSG_CUDA(cudaMemcpyAsync(out, fft->a.p, rb, cudaMemcpyDeviceToHost, fft->stream));
+    MUSG_CUDA(cudaStreamSynchronize(fft->stream));
+  });
+}
+
+int musg_projection_create(int dim, const int *resolutions, const double *lengths, int kind, int flags,
+                           musg_projection **out) {
+  return guard([&] {
+    require(out && resolutions, MUSG_ERR_ARGUMENT, "null argument");
+    require(kind >= 0 && kind <= 2, MUSG_ERR_ARGUMENT, "unknown projection kind");
+    if (!(flags & MUSG_FLAG_ALLOW_EVEN))
+      for (int d = 0; d < dim; ++d)
+        require(resolutions[d] % 2 == 1, MUSG_ERR_PROJECTION,
+                "Only an odd number of gridpoints in each direction is supported");
+    auto p = std::make_unique<musg_projection>();
+    p->kind = kind;
+    p->sp.init(dim, resolutions, dim * dim, kind, lengths, (flags & MUSG_FLAG_ALLOW_EVEN) != 0, false);
+    MUSG_CUDA(cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking));
+    *out = p.release();
+  });
+}
+
+int musg_projection_destroy(musg_projection *proj) {
+  return guard([&] { delete proj; });
+}
+
+int musg_projection_apply(musg_projection *proj, double *vec) {
+  return guard([&] {
+    require(proj && vec, MUSG_ERR_ARGUMENT, "null argument");
+    Spectral &sp = proj->sp;
+    const size_t rb = (size_t)sp.g.npx * sp.ncomp * sizeof(double);
+    if (proj->a.bytes < rb) proj->a.alloc(rb);
+    if (proj->b.bytes < rb) proj->b.alloc(rb);
+    MUSG_CUDA(cudaMemcpyAsync(proj->a.p, vec, rb, cudaMemcpyHostToDevice, proj->stream));
+    aos_to_soa(proj->a.as<double>(), proj->b.as<double>(), sp.ncomp, sp.g.npx, proj->stream);
+    spectral_project<double>(sp, proj->b.as<double>(), proj->b.as<double>(), 1.0, proj->stream);
+    soa_to_aos(proj->b.as<double>(), proj->a.as<double>(), sp.ncomp, sp.g.npx, proj->stream);
+    MUSG_CUDA(cudaMemcpyAsync(vec, proj->a.p, rb, cudaMemcpyDeviceToHost, proj->stream));
+    MUSG_CUDA(cudaStreamSynchronize(proj->stream));
+  });
+}
+
+int musg_projection_get_operator(musg_projection *proj, double *out, long long *rows, long long *cols) {
+  return guard([&] {
+    require(proj, MUSG_ERR_ARGUMENT, "null projection");
+    const Spectral &sp = proj->sp;
+    const int dim = sp.g.dim;
+    const long long nk = sp.g.nk;
+    const long long nrow = proj->kind == MUSG_PROJ_FINITE_STRAIN_FAST ? dim : (long long)dim * dim * dim * dim;
+    if (rows) *rows = nrow;
+    if (cols) *cols = nk;
+    if (!out) return;
+    // the operator as the reference stores it, computed on the host from the unit
+    // wave vectors (projection_small_strain.cc:56-86, projection_finite_strain.cc:62-95,
+    // projection_finite_strain_fast.cc:61-73)
+    int fres[3] = {sp.g.n[0], sp.g.n[1], sp.g.n[2]};
+    fres[dim - 1] = sp.g.nh;
+    auto freq = [](int n, int k) {
+      int N = (n - 1) / 2 + 1;
+      return k < N ? (double)k : (double)(-(n / 2) + k - N);
+    };
+    for (long long k = 0; k < nk; ++k) {
+      int cc[3] = {0, 0, 0};
+      long long t = k;
+      for (int d = dim - 1; d >= 0; --d) {
+        cc[d] = (int)(t % fres[d]);
+        t /= fres[d];
+      }
+      double xi[3] = {0, 0, 0}, nrm = 0;
+      bool zero = (k == 0);
+      for (int d = 0; d < dim; ++d) {
+        xi[d] = freq(sp.g.n[d], cc[d]) / sp.lengths[d];
+        nrm += xi[d] * xi[d];
+        if (sp.allow_even && sp.g.n[d] % 2 == 0 && cc[d] == sp.g.n[d] / 2) zero = true;
+      }
+      nrm = std::sqrt(nrm);
+      for (int d = 0; d < dim; ++d) xi[d] = zero ? 0.0 : xi[d] / nrm;
+      double *col = out + k * nrow;
+      if (proj->kind == MUSG_PROJ_FINITE_STRAIN_FAST) {
+        for (int d = 0; d < dim; ++d) col[d] = xi[d];
+        continue;
+      }
+      const int D = dim, D2 = dim * dim;
+      for (int m = 0; m < D; ++m)
+        for (int l = 0; l < D; ++l)
+          for (int j = 0; j < D; ++j)
+            for (int i = 0; i < D; ++i) {
+              double g;
+              if (proj->kind == MUSG_PROJ_SMALL_STRAIN) {
+                auto kr = [](int a, int b) { return a == b ? 1.0 : 0.0; };
+                g = 0.5 * (xi[i] * kr(j, l) * xi[m] + xi[i] * kr(j, m) * xi[l] + xi[j] * kr(i, l) * xi[m] +
+                           xi[j] * kr(i, m) * xi[l]) -
+                    xi[i] * xi[j] * xi[l] * xi[m];
+              } else {
+                g = (i == l ? 1.0 : 0.0) * xi[j] * xi[m];  // outer_under(I, xi xi^T)
+              }
+              col[(i + D * j) + D2 * (l + D * m)] = g;
+            }
+    }
+  });
+}
+
+}  // extern "C"

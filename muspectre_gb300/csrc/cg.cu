@@ -1,0 +1,225 @@
+// Conjugate-gradient vector and scalar kernels (src/solver/solver_cg.cc:54-110).
+//
+// The loop runs on the device: the CGState holds the FP64 scalars (r.r, alpha,
+// beta, the iteration count and an `active` flag).  Every kernel of an iteration
+// returns at once when `active` is 0, so a CUDA graph holding several iterations
+// can be replayed past convergence without changing the result.  Dot products are
+// reduced in two deterministic stages (fixed block partition, then one block in a
+// fixed order), so a rerun gives bit-identical scalars.  FP32 vectors are
+// accumulated with Neumaier-compensated FP32 sums per thread and FP64 across
+// threads and blocks.
+#include "spectral.cuh"
+
+namespace musg {
+
+constexpr int kRedThreads = 256;
+constexpr int kRedMaxBlocks = 2048;
+
+int reduce_blocks(long long n) {
+  long long b = (n + kRedThreads * 8 - 1) / (kRedThreads * 8);
+  if (b < 1) b = 1;
+  if (b > kRedMaxBlocks) b = kRedMaxBlocks;
+  return (int)b;
+}
+
+// deterministic sum of nparts doubles by one block
+__device__ __forceinline__ double sum_partials(const double *partial, int nparts) {
+  double v = 0.0;
+  for (int i = threadIdx.x; i < nparts; i += blockDim.x) v += partial[i];
+  return block_sum(v);
+}
+
+template <typename R>
+__global__ void k_cg_init(const double *__restrict__ rhs, R *__restrict__ r, R *__restrict__ x, long long n,
+                          double *partial, double *partial2) {
+  Acc<R> acc;
+  double acc2 = 0.0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const double b = rhs[i];
+    const R rv = R(-b);
+    r[i] = rv;
+    x[i] = R(0);
+    acc.add(rv * rv);
+    acc2 += b * b;
+  }
+  const double s1 = block_sum(acc.value());
+  if (threadIdx.x == 0) partial[blockIdx.x] = s1;
+  __syncthreads();
+  const double s2 = block_sum(acc2);
+  if (threadIdx.x == 0) partial2[blockIdx.x] = s2;
+}
+
+__global__ void k_cg_init_scalars(CGState *st, const double *partial, const double *partial2, int nparts,
+                                  double tol, int maxiter) {
+  const double rdr = sum_partials(partial, nparts);
+  __syncthreads();
+  const double rhs2 = sum_partials(partial2, nparts);
+  if (threadIdx.x == 0) {
+    st->rdr = rdr;
+    st->rhs_norm2 = rhs2;
+    st->tol2 = tol * tol * rhs2;
+    st->alpha = st->beta = st->pAp = 0.0;
+    st->iter = 0;
+    st->maxiter = maxiter;
+    // solver_cg.cc:76-77: i < maxiter && (rdr > tol2 || i == 0)
+    st->active = maxiter > 0 ? 1 : 0;
+  }
+}
+
+template <typename R>
+void cg_init(CGState *st, const double *rhs, R *r, R *x, long long n, double tol, int maxiter, double *partial,
+             double *partial2, cudaStream_t s) {
+  const int nb = reduce_blocks(n);
+  k_cg_init<R><<<nb, kRedThreads, 0, s>>>(rhs, r, x, n, partial, partial2);
+  MUSG_CHECK_LAUNCH();
+  k_cg_init_scalars<<<1, 1024, 0, s>>>(st, partial, partial2, nb, tol, maxiter);
+  MUSG_CHECK_LAUNCH();
+}
+
+// x += alpha p, r += alpha Ap, partial sums of r.r
+template <typename R>
+__global__ void k_cg_update(const CGState *__restrict__ st, R *__restrict__ x, R *__restrict__ r,
+                            const R *__restrict__ p, const R *__restrict__ Ap, long long n, double *partial) {
+  if (!st->active) return;
+  const R alpha = R(st->alpha);
+  Acc<R> acc;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    x[i] += alpha * p[i];
+    const R rv = r[i] + alpha * Ap[i];
+    r[i] = rv;
+    acc.add(rv * rv);
+  }
+  const double bs = block_sum(acc.value());
+  if (threadIdx.x == 0) partial[blockIdx.x] = bs;
+}
+
+template <typename R>
+void cg_update(const CGState *st, R *x, R *r, const R *p, const R *Ap, long long n, double *partial, cudaStream_t s) {
+  k_cg_update<R><<<reduce_blocks(n), kRedThreads, 0, s>>>(st, x, r, p, Ap, n, partial);
+  MUSG_CHECK_LAUNCH();
+}
+
+__global__ void k_cg_alpha(CGState *st, const double *partial, int nparts) {
+  if (!st->active) return;
+  const double pAp = sum_partials(partial, nparts);
+  if (threadIdx.x == 0) {
+    st->pAp = pAp;
+    st->alpha = st->rdr / pAp;  // solver_cg.cc:81
+  }
+}
+
+__global__ void k_cg_beta(CGState *st, const double *partial, int nparts) {
+  if (!st->active) return;
+  const double new_rdr = sum_partials(partial, nparts);
+  if (threadIdx.x == 0) {
+    st->beta = new_rdr / st->rdr;  // solver_cg.cc:86-88
+    st->rdr = new_rdr;
+    st->iter += 1;
+    st->counter += 1;
+    // loop condition for the next iteration (i >= 1 from here on); a non-finite
+    // residual fails the comparison and ends the loop, as in the reference
+    if (!(st->iter < st->maxiter && st->rdr > st->tol2)) st->active = 0;
+  }
+}
+
+void cg_finalize_alpha(CGState *st, const double *partial, int nparts, cudaStream_t s) {
+  k_cg_alpha<<<1, 1024, 0, s>>>(st, partial, nparts);
+  MUSG_CHECK_LAUNCH();
+}
+
+void cg_finalize_beta(CGState *st, const double *partial, int nparts, cudaStream_t s) {
+  k_cg_beta<<<1, 1024, 0, s>>>(st, partial, nparts);
+  MUSG_CHECK_LAUNCH();
+}
+
+// ------------------------------------------------------------------ dots
+template <typename Ra, typename Rb>
+__global__ void k_dot(const Ra *__restrict__ a, const Rb *__restrict__ b, long long n, double *partial) {
+  double acc = 0.0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    acc += (double)a[i] * (double)b[i];
+  const double bs = block_sum(acc);
+  if (threadIdx.x == 0) partial[blockIdx.x] = bs;
+}
+
+__global__ void k_sum_to(const double *partial, int nparts, double *out) {
+  const double v = sum_partials(partial, nparts);
+  if (threadIdx.x == 0) *out = v;
+}
+
+template <typename Ra, typename Rb>
+void dot_device(const Ra *a, const Rb *b, long long n, double *partial, double *out, cudaStream_t s) {
+  const int nb = reduce_blocks(n);
+  k_dot<Ra, Rb><<<nb, kRedThreads, 0, s>>>(a, b, n, partial);
+  MUSG_CHECK_LAUNCH();
+  k_sum_to<<<1, 1024, 0, s>>>(partial, nb, out);
+  MUSG_CHECK_LAUNCH();
+}
+
+// F += x; partial sums of x.x and F.F (after the update)
+template <typename R>
+__global__ void k_newton_update(double *__restrict__ F, const R *__restrict__ x, long long n, double *partial,
+                                int nparts) {
+  double axx = 0.0, aff = 0.0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const double xv = (double)x[i];
+    const double f = F[i] + xv;
+    F[i] = f;
+    axx += xv * xv;
+    aff += f * f;
+  }
+  const double s1 = block_sum(axx);
+  if (threadIdx.x == 0) partial[blockIdx.x] = s1;
+  __syncthreads();
+  const double s2 = block_sum(aff);
+  if (threadIdx.x == 0) partial[nparts + blockIdx.x] = s2;
+}
+
+__global__ void k_sum2_to(const double *partial, int nparts, double *out) {
+  const double a = sum_partials(partial, nparts);
+  __syncthreads();
+  const double b = sum_partials(partial + nparts, nparts);
+  if (threadIdx.x == 0) {
+    out[0] = a;
+    out[1] = b;
+  }
+}
+
+template <typename R>
+void newton_update(double *F, const R *x, long long n, double *partial, double *out, cudaStream_t s) {
+  const int nb = reduce_blocks(n);
+  k_newton_update<R><<<nb, kRedThreads, 0, s>>>(F, x, n, partial, nb);
+  MUSG_CHECK_LAUNCH();
+  k_sum2_to<<<1, 1024, 0, s>>>(partial, nb, out);
+  MUSG_CHECK_LAUNCH();
+}
+
+template <typename Rd, typename Rs>
+__global__ void k_convert(Rd *__restrict__ dst, const Rs *__restrict__ src, long long n, double scale) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    dst[i] = Rd((double)src[i] * scale);
+}
+
+template <typename Rd, typename Rs>
+void convert(Rd *dst, const Rs *src, long long n, double scale, cudaStream_t s) {
+  k_convert<Rd, Rs><<<reduce_blocks(n), kRedThreads, 0, s>>>(dst, src, n, scale);
+  MUSG_CHECK_LAUNCH();
+}
+
+template void cg_init<double>(CGState *, const double *, double *, double *, long long, double, int, double *,
+                              double *, cudaStream_t);
+template void cg_init<float>(CGState *, const double *, float *, float *, long long, double, int, double *, double *,
+                             cudaStream_t);
+template void cg_update<double>(const CGState *, double *, double *, const double *, const double *, long long,
+                                double *, cudaStream_t);
+template void cg_update<float>(const CGState *, float *, float *, const float *, const float *, long long, double *,
+                               cudaStream_t);
+template void dot_device<double, double>(const double *, const double *, long long, double *, double *, cudaStream_t);
+template void dot_device<float, float>(const float *, const float *, long long, double *, double *, cudaStream_t);
+template void newton_update<double>(double *, const double *, long long, double *, double *, cudaStream_t);
+template void newton_update<float>(double *, const float *, long long, double *, double *, cudaStream_t);
+template void convert<double, double>(double *, const double *, long long, double, cudaStream_t);
+template void convert<float, double>(float *, const double *, long long, double, cudaStream_t);
+template void convert<double, float>(double *, const float *, long long, double, cudaStream_t);
+
+}  // namespace musg

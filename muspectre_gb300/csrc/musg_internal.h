@@ -1,0 +1,235 @@
+// Internal declarations shared by the CUDA translation units and the host API of
+// libmusg.  Nothing here is part of the C ABI (include/musg.h is).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <cstdint>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/musg.h"
+
+namespace musg {
+
+struct Error : std::runtime_error {
+  int code;
+  Error(int c, const std::string &m) : std::runtime_error(m), code(c) {}
+};
+
+#define MUSG_CUDA(call)                                                              \
+  do {                                                                               \
+    cudaError_t e_ = (call);                                                         \
+    if (e_ != cudaSuccess)                                                           \
+      throw ::musg::Error(e_ == cudaErrorMemoryAllocation ? MUSG_ERR_MEMORY          \
+                                                          : MUSG_ERR_CUDA,           \
+                          std::string(#call) + ": " + cudaGetErrorString(e_));       \
+  } while (0)
+
+// kernels launched by the library in this process (graph replays add their nodes)
+extern std::atomic<unsigned long long> g_launches;
+
+#define MUSG_CHECK_LAUNCH()                 \
+  do {                                      \
+    ::musg::g_launches.fetch_add(1);        \
+    MUSG_CUDA(cudaGetLastError());          \
+  } while (0)
+
+template <typename R> struct V2;
+template <> struct V2<float> { using T = float2; };
+template <> struct V2<double> { using T = double2; };
+
+constexpr int kMaxStages = 16;
+constexpr int kMaxMaterials = 256;
+
+// ---------------------------------------------------------------- FFT plans
+// Device view of a 1-D FFT plan for one axis.  A length-n transform runs as a
+// Stockham mixed-radix FFT of length m (m == n), or, when n has a prime factor
+// above 7, as Bluestein's chirp-z algorithm over a 2/3/5/7-smooth m >= 2n-1.
+template <typename R> struct AxisPlanD {
+  int n;
+  int m;
+  int nst;
+  int blu;
+  unsigned long long rcode;  // radix of stage s in bits [4s, 4s+4)
+  const typename V2<R>::T *tw;    // m entries: exp(-2 pi i j / m)
+  const typename V2<R>::T *chirp; // n entries: exp(-pi i j^2 / n)     (Bluestein)
+  const typename V2<R>::T *bf;    // m entries: DFT_m(conj chirp)/m     (Bluestein)
+};
+
+struct AxisPlan {
+  int n = 0, m = 0, nst = 0, blu = 0;
+  int radix[kMaxStages] = {0};
+  // device tables, double and float copies
+  void *tw64 = nullptr, *chirp64 = nullptr, *bf64 = nullptr;
+  void *tw32 = nullptr, *chirp32 = nullptr, *bf32 = nullptr;
+  void build(int n);
+  void release();
+  template <typename R> AxisPlanD<R> device() const;
+};
+
+// ---------------------------------------------------------------- geometry
+struct Geom {
+  int dim = 0;
+  int n[3] = {1, 1, 1};     // real grid, row-major, n[dim-1] is the last axis
+  int nh = 0;               // n_last/2 + 1
+  long long npx = 0;        // pixels
+  long long nk = 0;         // hermitian k-points
+  long long nrows = 0;      // npx / n_last
+  int nlast() const { return n[dim - 1]; }
+};
+
+// Per-pixel tangent representation used by the CG operator (pass A prologue).
+enum TangentKind : int {
+  TK_PLAIN = 0,   // no tangent: input field copied (FFT engine / projection)
+  TK_SMALL = 1,   // small strain, isotropic: dP = lam tr(dF) I + mu (dF + dF^T)
+  TK_FINITE = 2,  // finite strain, isotropic PK2/GL: dP = dF S + F (lam tr(A) I + mu (A + A^T)), A = F^T dF
+  TK_KPRIME = 3,  // j-independent Kirchhoff tangent: dP(i,m) = sum_n K'(i,m,n) sum_j dF(j,n)
+  TK_MIXED = 4,   // per-pixel choice between TK_FINITE and TK_KPRIME by material law
+};
+
+// Device data the CG operator reads (precision R).
+template <typename R> struct TangentData {
+  const R *lam = nullptr;   // [npx]
+  const R *mu = nullptr;    // [npx]
+  const R *F = nullptr;     // [D*D][npx]  (finite strain)
+  const R *S = nullptr;     // [D*D][npx] PK2 stress (finite strain, isotropic)
+  const R *Kp = nullptr;    // [D^3][npx]  (Kirchhoff tangent)
+  const uint8_t *mat = nullptr;      // [npx] material index (TK_MIXED)
+  const uint8_t *law_kind = nullptr; // [kMaxMaterials]: TK_FINITE or TK_KPRIME (TK_MIXED)
+};
+
+// CG scalar state, resident on the device (all FP64).
+struct CGState {
+  double rdr;        // r.r of the current residual
+  double rhs_norm2;  // rhs.rhs
+  double tol2;       // tol^2 * rhs.rhs
+  double alpha, beta, pAp;
+  int iter;          // iterations of this solve
+  int maxiter;
+  int active;        // 1 while the loop runs
+  int pad;
+  unsigned long long counter;  // cumulative iterations (SolverBase::counter)
+};
+
+// ---------------------------------------------------------------- spectral ops
+// Workspace + plans for one grid; one instance per cell / FFT engine / projection.
+struct Spectral {
+  Geom g;
+  int ncomp = 0;            // components per pixel
+  int proj_kind = -1;       // MUSG_PROJ_* (-1: none)
+  bool allow_even = false;
+  double lengths[3] = {1, 1, 1};
+  AxisPlan ax[3];
+  // per-axis xi_d(k) = fftfreq_d(k)/L_d over the hermitian index range, FP64 and FP32
+  void *xi64[3] = {nullptr, nullptr, nullptr};
+  void *xi32[3] = {nullptr, nullptr, nullptr};
+  void *spec64 = nullptr;   // [ncomp][nk] complex double
+  void *spec32 = nullptr;   // [ncomp][nk] complex float
+  bool want32 = false;
+  void init(int dim, const int *res, int ncomp, int proj_kind, const double *lengths,
+            bool allow_even, bool want32);
+  void ensure32();
+  void release();
+};
+
+// Launch configuration limits of the pass kernels
+constexpr int kPassThreads = 512;
+
+// Pass launchers (spectral_*.cu).  All run on `stream`.
+//  fwd: real field [ncomp][npx] (scaled) -> spectrum (r2c over all axes)
+//  inv: spectrum -> real field (c2r, unnormalised, scaled)
+//  project: real -> real through the Green operator of sp.proj_kind
+template <typename R>
+void spectral_forward(Spectral &sp, const R *in, R scale, cudaStream_t s);
+template <typename R>
+void spectral_inverse(Spectral &sp, R *out, R scale, cudaStream_t s);
+template <typename R>
+void spectral_project(Spectral &sp, const R *in, R *out, R in_scale, cudaStream_t s);
+
+// CG operator application, fused: p = -r + beta p (or p = -r on the first
+// iteration), Ap = G(K:p), partial[b] = block sums of p.Ap.  Returns the number of
+// partial sums written (blocks of the last pass).
+// ev (optional): an event is recorded before the first and after every kernel
+template <typename R>
+int cg_operator(Spectral &sp, int tkind, const TangentData<R> &td, const CGState *st,
+                const R *r, R *p, R *Ap, double *partial, cudaStream_t s,
+                cudaEvent_t *ev = nullptr);
+// plain operator (no CG state): out = G(K:in)
+template <typename R>
+void tangent_operator(Spectral &sp, int tkind, const TangentData<R> &td, const R *in,
+                      R *out, cudaStream_t s);
+int cg_operator_partials(const Spectral &sp);
+
+// ---------------------------------------------------------------- CG kernels (cg.cu)
+int reduce_blocks(long long n);
+template <typename R>
+void cg_init(CGState *st, const double *rhs, R *r, R *x, long long n, double tol,
+             int maxiter, double *partial, double *partial2, cudaStream_t s);
+template <typename R>
+void cg_update(const CGState *st, R *x, R *r, const R *p, const R *Ap, long long n,
+               double *partial, cudaStream_t s);
+void cg_finalize_alpha(CGState *st, const double *partial, int nparts, cudaStream_t s);
+void cg_finalize_beta(CGState *st, const double *partial, int nparts, cudaStream_t s);
+// FP64 dot of a with b over n entries into *out_device (deterministic)
+template <typename Ra, typename Rb>
+void dot_device(const Ra *a, const Rb *b, long long n, double *partial, double *out,
+                cudaStream_t s);
+// y += x (promoting), with the dots x.x and y.y (after the update) into out[0], out[1]
+template <typename R>
+void newton_update(double *F, const R *x, long long n, double *partial, double *out,
+                   cudaStream_t s);
+template <typename Rd, typename Rs>
+void convert(Rd *dst, const Rs *src, long long n, double scale, cudaStream_t s);
+
+// ---------------------------------------------------------------- materials (materials.cu)
+struct MatParams {
+  int law;
+  int logm_mode;            // HEP1: 0 projector sum (reference), 1 spectral
+  double lam, mu, K, tau_y0, H;
+};
+
+struct MaterialArgs {
+  int dim, form;
+  long long npx;
+  const double *F;          // [D*D][npx]
+  double *P;                // [D*D][npx]
+  const uint8_t *mat;       // [npx]
+  const MatParams *params;  // [nmat]
+  const double *lam, *mu;   // [npx] (elastic laws)
+  const double *eig;        // [D*D][npx] eigenstrain (LE2), may be null
+  // HEP1 state, two buffers each; cur selects the current one
+  double *Fprev[2], *be[2], *eps[2];
+  int cur;
+  // tangent outputs in CG precision (float or double, one of them set)
+  double *S64, *Kp64, *Fc64;
+  float *S32, *Kp32, *Fc32;
+  double *Kfull;            // optional full tangent, AoS [npx][D^4] (API)
+  int *nonfinite;           // device flag set when a non-finite stress appears
+};
+void material_evaluate(const MaterialArgs &a, cudaStream_t s);
+void add_macro(double *F, const double *delta_dev, int ncomp, long long npx, cudaStream_t s);
+void fill_uniform(double *F, const double *value_dev, int ncomp, long long npx, cudaStream_t s);
+
+// AoS (host layout, pixel-major) <-> SoA (component planes) on the device
+void aos_to_soa(const double *aos, double *soa, int ncomp, long long npx, cudaStream_t s);
+void soa_to_aos(const double *soa, double *aos, int ncomp, long long npx, cudaStream_t s);
+void soa_to_aos_complex(const double2 *soa, double2 *aos, int ncomp, long long nk, cudaStream_t s);
+void aos_to_soa_complex(const double2 *aos, double2 *soa, int ncomp, long long nk, cudaStream_t s);
+
+// simple device buffer
+struct DevBuf {
+  void *p = nullptr;
+  size_t bytes = 0;
+  void alloc(size_t b);
+  void release();
+  template <typename T> T *as() const { return reinterpret_cast<T *>(p); }
+  ~DevBuf() { release(); }
+  DevBuf() = default;
+  DevBuf(const DevBuf &) = delete;
+  DevBuf &operator=(const DevBuf &) = delete;
+};
+
+}  // namespace musg

@@ -1,0 +1,325 @@
+// Host launchers of the spectral passes, instantiated once per precision by
+// spectral_f64.cu and spectral_f32.cu.
+#pragma once
+
+#include <algorithm>
+#include <mutex>
+#include <set>
+
+#include "spectral.cuh"
+
+namespace musg {
+
+namespace {
+
+int optin_smem() {
+  static int v = 0;
+  if (v == 0) {
+    int dev = 0;
+    MUSG_CUDA(cudaGetDevice(&dev));
+    int b = 0;
+    MUSG_CUDA(cudaDeviceGetAttribute(&b, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    v = b - 2048;  // room for the static shared memory of the reductions
+  }
+  return v;
+}
+
+// raise the dynamic shared-memory limit of a kernel once (keyed by its address)
+template <typename K> void allow_smem(K kernel) {
+  static std::mutex mu;
+  static std::set<const void *> done;
+  const void *key = (const void *)kernel;
+  std::lock_guard<std::mutex> lock(mu);
+  if (done.count(key)) return;
+  MUSG_CUDA(cudaFuncSetAttribute(key, cudaFuncAttributeMaxDynamicSharedMemorySize, optin_smem()));
+  done.insert(key);
+}
+
+// complex elements per block the configurations aim for (latency hiding vs. the
+// number of blocks)
+constexpr long kTargetElems = 8192;
+
+struct Cfg {
+  int per;       // rows per block (last pass) or tile (axis / green passes)
+  int blocks;
+  size_t smem;
+};
+
+// shared memory per block: two ping-pong buffers of (pencils x m) complex values
+template <typename R> Cfg last_cfg(const Spectral &sp) {
+  const AxisPlan &ap = sp.ax[sp.g.dim - 1];
+  const long per_pair = (long)sp.ncomp * ap.m;
+  const long eb = 2 * sizeof(typename V2<R>::T);
+  long g2 = std::min(kTargetElems / per_pair, (long)optin_smem() / (per_pair * eb));
+  if (g2 < 1) throw Error(MUSG_ERR_ARGUMENT, "last-axis FFT too long for one thread block");
+  g2 = std::min<long>(g2, 16);
+  g2 = std::min<long>(g2, (sp.g.nrows + 1) / 2);
+  Cfg c;
+  c.per = (int)(2 * g2);
+  c.blocks = (int)((sp.g.nrows + c.per - 1) / c.per);
+  c.smem = (size_t)(g2 * per_pair * eb);
+  return c;
+}
+
+template <typename R> Cfg axis_cfg(const Spectral &sp, int axis, long long inner, long long nbatch) {
+  const AxisPlan &ap = sp.ax[axis];
+  const long eb = 2 * sizeof(typename V2<R>::T);
+  long T = std::min(kTargetElems / ap.m, (long)optin_smem() / (ap.m * eb));
+  if (T < 1) throw Error(MUSG_ERR_ARGUMENT, "FFT axis too long for one thread block");
+  T = std::min<long>(T, 32);
+  if (T > 8) T &= ~3L;
+  T = std::min<long>(T, inner);
+  Cfg c;
+  c.per = (int)T;
+  const long long ntiles = (inner + T - 1) / T;
+  c.blocks = (int)(ntiles * nbatch);
+  c.smem = (size_t)(T * ap.m * eb);
+  return c;
+}
+
+template <typename R> Cfg green_cfg(const Spectral &sp, long long Rr) {
+  const AxisPlan &ap = sp.ax[0];
+  const long per = (long)sp.ncomp * ap.m;
+  const long eb = 2 * sizeof(typename V2<R>::T);
+  long T = std::min(kTargetElems / per, (long)optin_smem() / (per * eb));
+  if (T < 1) throw Error(MUSG_ERR_ARGUMENT, "first-axis FFT too long for one thread block");
+  T = std::min<long>(T, 32);
+  if (T > 8) T &= ~3L;
+  T = std::min<long>(T, Rr);
+  Cfg c;
+  c.per = (int)T;
+  c.blocks = (int)((Rr + T - 1) / T);
+  c.smem = (size_t)(T * per * eb);
+  return c;
+}
+
+template <typename R> typename V2<R>::T *spec_of(Spectral &sp);
+template <> inline double2 *spec_of<double>(Spectral &sp) { return (double2 *)sp.spec64; }
+template <> inline float2 *spec_of<float>(Spectral &sp) {
+  sp.ensure32();
+  return (float2 *)sp.spec32;
+}
+template <typename R> const R *xi_of(const Spectral &sp, int d);
+template <> inline const double *xi_of<double>(const Spectral &sp, int d) { return (const double *)sp.xi64[d]; }
+template <> inline const float *xi_of<float>(const Spectral &sp, int d) { return (const float *)sp.xi32[d]; }
+
+template <typename R> LastArgs<R> last_args(Spectral &sp, const Cfg &c) {
+  LastArgs<R> a{};
+  a.ap = sp.ax[sp.g.dim - 1].device<R>();
+  a.L = sp.g.nlast();
+  a.H = sp.g.nh;
+  a.G = c.per;
+  a.ncomp = sp.ncomp;
+  a.nrows = sp.g.nrows;
+  a.npx = sp.g.npx;
+  a.nk = sp.g.nk;
+  a.spec = spec_of<R>(sp);
+  return a;
+}
+
+template <typename R, int PRO, int D, int TK>
+void launch_fwd(const LastArgs<R> &a, const Cfg &c, cudaStream_t s) {
+  auto k = k_last_fwd<R, PRO, D, TK>;
+  allow_smem(k);
+  k<<<c.blocks, kPassThreads, c.smem, s>>>(a);
+  MUSG_CHECK_LAUNCH();
+}
+
+template <typename R, int PRO>
+void dispatch_fwd(int dim, int tk, const LastArgs<R> &a, const Cfg &c, cudaStream_t s) {
+  if (PRO == PRO_PLAIN) {
+    launch_fwd<R, PRO_PLAIN, 0, TK_PLAIN>(a, c, s);
+    return;
+  }
+#define MUSG_FWD_CASE(DD, TT) \
+  if (dim == DD && tk == TT) { launch_fwd<R, PRO, DD, TT>(a, c, s); return; }
+  MUSG_FWD_CASE(2, TK_SMALL) MUSG_FWD_CASE(2, TK_FINITE) MUSG_FWD_CASE(2, TK_KPRIME) MUSG_FWD_CASE(2, TK_MIXED)
+  MUSG_FWD_CASE(3, TK_SMALL) MUSG_FWD_CASE(3, TK_FINITE) MUSG_FWD_CASE(3, TK_KPRIME) MUSG_FWD_CASE(3, TK_MIXED)
+#undef MUSG_FWD_CASE
+  throw Error(MUSG_ERR_ARGUMENT, "unsupported tangent kind");
+}
+
+template <typename R, int EPI, int D>
+void launch_inv(const LastArgs<R> &a, const Cfg &c, cudaStream_t s) {
+  auto k = k_last_inv<R, EPI, D>;
+  allow_smem(k);
+  k<<<c.blocks, kPassThreads, c.smem, s>>>(a);
+  MUSG_CHECK_LAUNCH();
+}
+
+template <typename R>
+void run_axis(Spectral &sp, bool inv, const CGState *st, cudaStream_t s) {
+  // 3-D only: pencils along axis 1 of [c][k0][k1][k2h]
+  const long long inner = sp.g.nh;
+  const long long nbatch = (long long)sp.ncomp * sp.g.n[0];
+  const Cfg c = axis_cfg<R>(sp, 1, inner, nbatch);
+  AxisArgs<R> a{};
+  a.ap = sp.ax[1].device<R>();
+  a.nax = sp.g.n[1];
+  a.T = c.per;
+  a.ntiles = (int)((inner + c.per - 1) / c.per);
+  a.se = sp.g.nh;
+  a.inner = inner;
+  a.sb = (long long)sp.g.n[1] * sp.g.nh;
+  a.spec = spec_of<R>(sp);
+  a.st = st;
+  if (inv) {
+    auto k = k_axis<R, true>;
+    allow_smem(k);
+    k<<<c.blocks, kPassThreads, c.smem, s>>>(a);
+  } else {
+    auto k = k_axis<R, false>;
+    allow_smem(k);
+    k<<<c.blocks, kPassThreads, c.smem, s>>>(a);
+  }
+  MUSG_CHECK_LAUNCH();
+}
+
+template <typename R>
+void run_green(Spectral &sp, int mode, const CGState *st, cudaStream_t s) {
+  const int dim = sp.g.dim;
+  const long long Rr = sp.g.nk / sp.g.n[0];
+  const Cfg c = green_cfg<R>(sp, Rr);
+  GreenArgs<R> a{};
+  a.ap = sp.ax[0].device<R>();
+  a.n0 = sp.g.n[0];
+  a.T = c.per;
+  a.ncomp = sp.ncomp;
+  a.n1 = sp.g.n[1];
+  a.nh = sp.g.nh;
+  a.Rr = Rr;
+  a.nk = sp.g.nk;
+  a.spec = spec_of<R>(sp);
+  a.xi0 = xi_of<R>(sp, 0);
+  a.xi1 = xi_of<R>(sp, 1);
+  a.xi2 = dim == 3 ? xi_of<R>(sp, 2) : nullptr;
+  auto nyq = [&](int d) { return (sp.allow_even && sp.g.n[d] % 2 == 0) ? sp.g.n[d] / 2 : -1; };
+  a.nyq0 = nyq(0);
+  a.nyq1 = nyq(1);
+  a.nyq2 = dim == 3 ? nyq(2) : -1;
+  a.norm = R(1.0 / (double)sp.g.npx);
+  a.st = st;
+#define MUSG_GREEN(MODE, DD)                                     \
+  {                                                              \
+    auto k = k_green<R, MODE, DD>;                               \
+    allow_smem(k);                                               \
+    k<<<c.blocks, kPassThreads, c.smem, s>>>(a);                 \
+  }
+  if (mode == GM_FWD) MUSG_GREEN(GM_FWD, 2)
+  else if (mode == GM_INV) MUSG_GREEN(GM_INV, 2)
+  else if (mode == GM_SMALL && dim == 2) MUSG_GREEN(GM_SMALL, 2)
+  else if (mode == GM_SMALL && dim == 3) MUSG_GREEN(GM_SMALL, 3)
+  else if (mode == GM_FINITE && dim == 2) MUSG_GREEN(GM_FINITE, 2)
+  else if (mode == GM_FINITE && dim == 3) MUSG_GREEN(GM_FINITE, 3)
+  else throw Error(MUSG_ERR_ARGUMENT, "unsupported projection");
+#undef MUSG_GREEN
+  MUSG_CHECK_LAUNCH();
+}
+
+int green_mode_of(const Spectral &sp) {
+  if (sp.proj_kind == MUSG_PROJ_SMALL_STRAIN) return GM_SMALL;
+  if (sp.proj_kind == MUSG_PROJ_FINITE_STRAIN_FAST || sp.proj_kind == MUSG_PROJ_FINITE_STRAIN) return GM_FINITE;
+  throw Error(MUSG_ERR_PROJECTION, "no projection operator attached to this spectral workspace");
+}
+
+}  // namespace
+
+template <typename R>
+void spectral_forward(Spectral &sp, const R *in, R scale, cudaStream_t s) {
+  const Cfg c = last_cfg<R>(sp);
+  LastArgs<R> a = last_args<R>(sp, c);
+  a.in = in;
+  a.scale = scale;
+  dispatch_fwd<R, PRO_PLAIN>(sp.g.dim, TK_PLAIN, a, c, s);
+  if (sp.g.dim == 3) run_axis<R>(sp, false, nullptr, s);
+  run_green<R>(sp, GM_FWD, nullptr, s);
+}
+
+template <typename R>
+void spectral_inverse(Spectral &sp, R *out, R scale, cudaStream_t s) {
+  run_green<R>(sp, GM_INV, nullptr, s);
+  if (sp.g.dim == 3) run_axis<R>(sp, true, nullptr, s);
+  const Cfg c = last_cfg<R>(sp);
+  LastArgs<R> a = last_args<R>(sp, c);
+  a.out = out;
+  a.scale = scale;
+  launch_inv<R, EPI_PLAIN, 0>(a, c, s);
+}
+
+template <typename R>
+void spectral_project(Spectral &sp, const R *in, R *out, R in_scale, cudaStream_t s) {
+  const int gm = green_mode_of(sp);
+  const Cfg c = last_cfg<R>(sp);
+  LastArgs<R> a = last_args<R>(sp, c);
+  a.in = in;
+  a.out = out;
+  a.scale = in_scale;
+  dispatch_fwd<R, PRO_PLAIN>(sp.g.dim, TK_PLAIN, a, c, s);
+  if (sp.g.dim == 3) run_axis<R>(sp, false, nullptr, s);
+  run_green<R>(sp, gm, nullptr, s);
+  if (sp.g.dim == 3) run_axis<R>(sp, true, nullptr, s);
+  a.scale = R(1);
+  launch_inv<R, EPI_PLAIN, 0>(a, c, s);
+}
+
+template <typename R>
+int cg_operator(Spectral &sp, int tkind, const TangentData<R> &td, const CGState *st, const R *r, R *p,
+                R *Ap, double *partial, cudaStream_t s, cudaEvent_t *ev) {
+  const int gm = green_mode_of(sp);
+  const Cfg c = last_cfg<R>(sp);
+  LastArgs<R> a = last_args<R>(sp, c);
+  a.st = st;
+  a.r = r;
+  a.p = p;
+  a.Ap = Ap;
+  a.partial = partial;
+  a.td = td;
+  int k = 0;
+  auto mark = [&]() {
+    if (ev) MUSG_CUDA(cudaEventRecord(ev[k++], s));
+  };
+  mark();
+  dispatch_fwd<R, PRO_CG>(sp.g.dim, tkind, a, c, s);
+  mark();
+  if (sp.g.dim == 3) {
+    run_axis<R>(sp, false, st, s);
+    mark();
+  }
+  run_green<R>(sp, gm, st, s);
+  mark();
+  if (sp.g.dim == 3) {
+    run_axis<R>(sp, true, st, s);
+    mark();
+  }
+  if (sp.g.dim == 2) launch_inv<R, EPI_CG, 2>(a, c, s);
+  else launch_inv<R, EPI_CG, 3>(a, c, s);
+  mark();
+  return c.blocks;
+}
+
+template <typename R>
+void tangent_operator(Spectral &sp, int tkind, const TangentData<R> &td, const R *in, R *out, cudaStream_t s) {
+  const int gm = green_mode_of(sp);
+  const Cfg c = last_cfg<R>(sp);
+  LastArgs<R> a = last_args<R>(sp, c);
+  a.in = in;
+  a.out = out;
+  a.scale = R(1);
+  a.td = td;
+  dispatch_fwd<R, PRO_TANGENT>(sp.g.dim, tkind, a, c, s);
+  if (sp.g.dim == 3) run_axis<R>(sp, false, nullptr, s);
+  run_green<R>(sp, gm, nullptr, s);
+  if (sp.g.dim == 3) run_axis<R>(sp, true, nullptr, s);
+  launch_inv<R, EPI_PLAIN, 0>(a, c, s);
+}
+
+#define MUSG_INSTANTIATE_SPECTRAL(R)                                                               \
+  template void spectral_forward<R>(Spectral &, const R *, R, cudaStream_t);                      \
+  template void spectral_inverse<R>(Spectral &, R *, R, cudaStream_t);                            \
+  template void spectral_project<R>(Spectral &, const R *, R *, R, cudaStream_t);                 \
+  template int cg_operator<R>(Spectral &, int, const TangentData<R> &, const CGState *, const R *, \
+                              R *, R *, double *, cudaStream_t, cudaEvent_t *);                    \
+  template void tangent_operator<R>(Spectral &, int, const TangentData<R> &, const R *, R *,       \
+                                    cudaStream_t);
+
+}  // namespace musg

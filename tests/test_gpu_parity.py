@@ -1,0 +1,458 @@
+"""GPU parity: the CUDA path (through the C ABI) against the CPU oracle and the
+reference's golden vectors.  Tolerances are the reference tests' own (FFT 1e-14·N,
+projection 1e-12·N, material KATs 1e-8) or, for full Newton-CG solves in FP64, 1e-10
+relative on the fields with identical Newton and CG iteration counts.
+"""
+import itertools
+import json
+import os
+
+import numpy as np
+import pytest
+
+from oracle import muspectre_oracle as o
+
+pytestmark = pytest.mark.gpu
+
+GOLD = os.path.join(os.path.dirname(__file__), 'golden')
+
+
+@pytest.fixture(scope='module')
+def mu():
+    import muspectre_gb300 as m
+    if m.device_count() < 1:
+        pytest.fail('no CUDA device visible')
+    return m
+
+
+def rel(a, b):
+    a = np.asarray(a, dtype=float)
+    b = np.asarray(b, dtype=float)
+    return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)
+
+
+# ------------------------------------------------------------------ FFT engine
+@pytest.mark.parametrize('res', [[6, 4], [5, 7], [51, 51], [17, 13], [8, 6, 4], [5, 7, 9], [15, 11, 13],
+                                 [16, 16, 16], [34, 21], [64, 64, 64]])
+def test_fft_vs_numpy(mu, res):
+    """python_fft_tests.py:60-101 (tolerance 1e-14·N), over radix-2/3/5/7 and
+    Bluestein lengths (11, 13, 17, 51 = 3·17, 34 = 2·17)."""
+    rng = np.random.default_rng(len(res) * 100 + res[0])
+    dim = len(res)
+    eng = mu.fft.FFT(res, dim * dim)
+    N = int(np.prod(res))
+    tol = 1e-14 * N
+    in_arr = rng.random([*res, dim, dim])
+    out_ref = np.fft.rfftn(in_arr, axes=tuple(range(dim)))
+    out = eng.fft(in_arr.reshape(-1, dim * dim).T).T
+    assert np.linalg.norm(out_ref - out.reshape(out_ref.shape)) < tol * max(1.0, np.abs(out_ref).max() / N)
+    cres = mu.get_hermitian_sizes(res)
+    c = rng.random([*cres, dim, dim]) + 1j * rng.random([*cres, dim, dim])
+    ref = np.fft.irfftn(c, s=res, axes=tuple(range(dim)))
+    back = eng.ifft(c.reshape(-1, dim * dim).T).T * eng.normalisation()
+    assert np.linalg.norm(ref - back.reshape(ref.shape)) < tol
+
+
+def test_fft_round_trip_large(mu):
+    """round trip ifft(fft(x))/N = x at 128³ with 9 components (size-independent)."""
+    res = [128, 128, 128]
+    rng = np.random.default_rng(5)
+    eng = mu.fft.FFT(res, 9)
+    x = rng.standard_normal((9, int(np.prod(res))))
+    y = eng.ifft(eng.fft(x)) * eng.normalisation()
+    assert np.max(np.abs(x - y)) < 1e-13
+
+
+# ------------------------------------------------------------------ projections
+GOOSE = np.load(os.path.join(GOLD, 'goose_projection.npz'))
+
+
+@pytest.mark.parametrize('ndim', [2, 3])
+@pytest.mark.parametrize('kind,cls', [('small', 'ProjectionSmallStrain'), ('finite', 'ProjectionFiniteStrain'),
+                                      ('finite', 'ProjectionFiniteStrainFast')])
+def test_projection_vs_goose(mu, ndim, kind, cls):
+    """python_projection_tests.py:99-130 on the GPU projections (1e-12·N)."""
+    strain_g = GOOSE['%s_%dd_strain' % (kind, ndim)]
+    b_g = GOOSE['%s_%dd_result' % (kind, ndim)]
+    shape = [5] * ndim
+    proj = getattr(mu.fft, '%s_%dd' % (cls, ndim))(shape, shape)
+    proj.initialise()
+    tol = 1e-12 * np.prod(shape)
+    strain_mu = np.zeros((*shape, ndim, ndim))
+    for ijk in itertools.product(range(5), repeat=ndim):
+        strain_mu[ijk] = strain_g[(slice(None), slice(None), *ijk)].T
+    b_mu = proj.apply_projection(strain_mu.reshape(np.prod(shape), ndim ** 2).T).T.reshape(strain_mu.shape)
+    for ijk in itertools.product(range(5), repeat=ndim):
+        assert np.linalg.norm(b_mu[ijk].T - b_g[(slice(None), slice(None), *ijk)]) < tol
+
+
+@pytest.mark.parametrize('ndim', [2, 3])
+@pytest.mark.parametrize('kind', ['small', 'finite_full', 'finite_fast'])
+def test_projection_operator_vs_oracle(mu, ndim, kind):
+    shape = [5, 7, 9][:ndim]
+    lengths = [1.3, 2.0, 0.7][:ndim]
+    cls = {'small': 'ProjectionSmallStrain', 'finite_full': 'ProjectionFiniteStrain',
+           'finite_fast': 'ProjectionFiniteStrainFast'}[kind]
+    proj = getattr(mu.fft, '%s_%dd' % (cls, ndim))(shape, lengths)
+    ref = o.Projection(shape, lengths, kind)
+    assert np.max(np.abs(proj.get_operator() - ref.get_operator())) < 1e-14
+    rng = np.random.default_rng(ndim)
+    f = rng.standard_normal(int(np.prod(shape)) * ndim * ndim)
+    got = proj.apply_projection(f.reshape(-1, ndim * ndim).T).T.reshape(-1)
+    assert rel(got, ref.apply(f)) < 1e-13
+
+
+@pytest.mark.parametrize('res', [[4, 4, 4], [6, 6, 6], [8, 8, 8], [6, 5], [128, 128, 128]])
+@pytest.mark.parametrize('kind', ['small', 'finite_fast'])
+def test_even_extension(mu, res, kind):
+    """Even grids (extension): idempotence G(Gf) = Gf, agreement with the oracle's
+    extension at small sizes."""
+    dim = len(res)
+    cls = 'ProjectionSmallStrain' if kind == 'small' else 'ProjectionFiniteStrainFast'
+    proj = getattr(mu.fft, '%s_%dd' % (cls, dim))(res, [1.0] * dim, allow_even=True)
+    rng = np.random.default_rng(0)
+    n = int(np.prod(res))
+    f = rng.standard_normal((dim * dim, n))
+    g1 = proj.apply_projection(f)
+    g2 = proj.apply_projection(g1)
+    assert np.linalg.norm(g2 - g1) < 1e-12 * np.linalg.norm(g1)
+    if n <= 1000:
+        ref = o.Projection(res, [1.0] * dim, kind, allow_even=True)
+        assert rel(g1.T.reshape(-1), ref.apply(f.T.reshape(-1))) < 1e-13
+    with pytest.raises(mu.ProjectionError):
+        getattr(mu.fft, '%s_%dd' % (cls, dim))(res, [1.0] * dim)
+
+
+# ------------------------------------------------------------------ materials
+def _random_cell_pair(mu, res, form, seed, laws=('le1', 'le2', 'le3', 'le4'), hep=False):
+    """Same random microstructure in the oracle and on the GPU."""
+    rng = np.random.default_rng(seed)
+    dim = len(res)
+    n = int(np.prod(res))
+    lengths = [1.0 + 0.1 * d for d in range(dim)]
+    ocell = o.Cell(res, lengths, form)
+    gcell = mu.Cell(res, lengths, mu.Formulation(form))
+    owner = rng.integers(0, len(laws), n)
+    for k, law in enumerate(laws):
+        idx = np.flatnonzero(owner == k)
+        E, nu = float(rng.uniform(1, 10)), float(rng.uniform(0.2, 0.4))
+        D = dim
+        if law == 'le1':
+            om = ocell.add_material(o.MaterialLinearElastic1('m%d' % k, D, E, nu))
+            gm = getattr(mu.material, 'MaterialLinearElastic1_%dd' % D).make(gcell, 'm%d' % k, E, nu)
+            for i in idx:
+                om.add_pixel(i)
+            gm.add_pixels(idx)
+        elif law == 'le2':
+            om = ocell.add_material(o.MaterialLinearElastic2('m%d' % k, D, E, nu))
+            gm = getattr(mu.material, 'MaterialLinearElastic2_%dd' % D).make(gcell, 'm%d' % k, E, nu)
+            eig = rng.standard_normal((idx.size, D, D)) * 1e-3
+            eig = 0.5 * (eig + eig.transpose(0, 2, 1))
+            for i, e in zip(idx, eig):
+                om.add_pixel(i, e)
+            gm.add_pixels(idx, eig)
+        elif law in ('le3', 'le4'):
+            cls = o.MaterialLinearElastic3 if law == 'le3' else o.MaterialLinearElastic4
+            om = ocell.add_material(cls('m%d' % k, D))
+            gm = getattr(mu.material, 'MaterialLinearElastic%s_%dd' % (law[-1], D)).make(gcell, 'm%d' % k)
+            Es = rng.uniform(1, 10, idx.size)
+            nus = rng.uniform(0.2, 0.4, idx.size)
+            for i, e, v in zip(idx, Es, nus):
+                om.add_pixel(i, e, v)
+            gm.add_pixels(idx, Es, nus)
+        elif law == 'hep1':
+            tau_y0, H = 0.01 * E, 0.1 * E
+            om = ocell.add_material(o.MaterialHyperElastoPlastic1('m%d' % k, D, E, nu, tau_y0, H))
+            gm = getattr(mu.material, 'MaterialHyperElastoPlastic1_%dd' % D).make(gcell, 'm%d' % k, E, nu,
+                                                                                    tau_y0, H)
+            for i in idx:
+                om.add_pixel(i)
+            gm.add_pixels(idx)
+    return ocell, gcell, rng
+
+
+@pytest.mark.parametrize('dim', [2, 3])
+@pytest.mark.parametrize('form', [o.SMALL_STRAIN, o.FINITE_STRAIN])
+def test_material_stress_tangent(mu, dim, form):
+    """material_muSpectre_base.hh:292-401 for LE1-4: P and K per pixel vs the oracle."""
+    res = [7, 5, 3][:dim]
+    ocell, gcell, rng = _random_cell_pair(mu, res, form, 11 + dim)
+    n = ocell.n_px
+    F = rng.standard_normal((n, dim, dim)) * 0.05
+    if form == o.FINITE_STRAIN:
+        F += np.eye(dim)
+    ocell.F = o.t2_to_vec(F)
+    P, K = ocell.evaluate_stress_tangent()
+    gP, gK = gcell.evaluate_stress_tangent(o.t2_to_vec(F).reshape(n, -1).T, return_tangent=True)
+    assert rel(gP.T.reshape(-1), P) < 1e-14
+    assert rel(gK.T.reshape(-1), o.t4_to_vec(K)) < 1e-14
+
+
+@pytest.mark.parametrize('dim', [2, 3])
+@pytest.mark.parametrize('form', [o.SMALL_STRAIN, o.FINITE_STRAIN])
+def test_directional_stiffness(mu, dim, form):
+    """cell_base.cc:150-192: G(K:δF) vs the oracle."""
+    res = [7, 5, 3][:dim]
+    ocell, gcell, rng = _random_cell_pair(mu, res, form, 21 + dim)
+    n = ocell.n_px
+    F = rng.standard_normal((n, dim, dim)) * 0.05 + (np.eye(dim) if form == o.FINITE_STRAIN else 0)
+    ocell.F = o.t2_to_vec(F)
+    ocell.evaluate_stress_tangent()
+    gcell.evaluate_stress_tangent(o.t2_to_vec(F).reshape(n, -1).T)
+    dF = rng.standard_normal(n * dim * dim)
+    ref = ocell.directional_stiffness(dF)
+    got = gcell.directional_stiffness(dF.reshape(n, -1).T).T.reshape(-1)
+    assert rel(got, ref) < 1e-13
+
+
+def test_hep1_kat_on_gpu(mu):
+    """test_material_hyper_elasto_plastic1.cc:85-339 through a one-pixel GPU cell:
+    the cell's stress is PK1 = τ F⁻ᵀ; the KAT's τ is recovered as P Fᵀ."""
+    with open(os.path.join(GOLD, 'hep1_kat.json')) as f:
+        d = json.load(f)
+    E = o.young_from_K_mu(d['K'], d['mu'])
+    nu = o.poisson_from_K_mu(d['K'], d['mu'])
+    cell = mu.Cell([1, 1, 1], [1., 1., 1.], mu.Formulation.finite_strain)
+    mat = mu.material.MaterialHyperElastoPlastic1_3d.make(cell, 'Name', E, nu, d['tau_y0'], d['H'])
+    mat.add_pixel([0, 0, 0])
+    cell.initialise()
+    omat = o.MaterialHyperElastoPlastic1('Name', 3, E, nu, d['tau_y0'], d['H'])
+    omat.add_pixel(0)
+    omat.initialise()
+    F = np.eye(3)
+    for step in d['steps']:
+        F[0, 1] = step['F01']
+        P, K = cell.evaluate_stress_tangent(F.T.reshape(-1, 1), return_tangent=True)
+        Pm = P[:, 0].reshape(3, 3).T
+        tau = Pm @ F.T
+        assert np.linalg.norm(tau - np.array(step['tau'])) < d['tol']
+        # the golden Kirchhoff tangent is pinned on the oracle (CPU test); here the
+        # GPU's PK1 tangent (materials_toolbox.hh:374-410) is checked against the
+        # oracle's from the same state
+        _, Ko = omat.evaluate(F[None], o.FINITE_STRAIN)
+        Kg = K[:, 0].reshape(3, 3, 3, 3, order='F')
+        assert np.linalg.norm(Kg - Ko[0]) < 1e-12 * np.linalg.norm(Ko[0])
+        cell.save_history_variables()
+        omat.save_history_variables()
+
+
+def test_hep1_cell_vs_oracle(mu):
+    """HyperElastoPlastic1 in a heterogeneous cell with random F over two load
+    evaluations, including the state cycling (statefield.hh:322-326)."""
+    res = [5, 3, 3]
+    ocell, gcell, rng = _random_cell_pair(mu, res, o.FINITE_STRAIN, 7, laws=('hep1', 'hep1', 'le1'))
+    n = ocell.n_px
+    for it in range(3):
+        F = np.eye(3) + rng.standard_normal((n, 3, 3)) * 0.02 * (it + 1)
+        ocell.F = o.t2_to_vec(F)
+        P, K = ocell.evaluate_stress_tangent()
+        gP, gK = gcell.evaluate_stress_tangent(o.t2_to_vec(F).reshape(n, -1).T, return_tangent=True)
+        assert rel(gP.T.reshape(-1), P) < 1e-11
+        assert rel(gK.T.reshape(-1), o.t4_to_vec(K)) < 1e-10
+        if it == 1:
+            ocell.save_history_variables()
+            gcell.save_history_variables()
+
+
+# ------------------------------------------------------------------ solves
+def _readme_pair(mu):
+    """README:44-80 (51×51, small strain, LE1 hard/soft disc)."""
+    res = [51, 51]
+    lengths = [7., 5.]
+    ocell = o.Cell(res, lengths, o.SMALL_STRAIN)
+    gcell = mu.SystemFactory(res, lengths, mu.Formulation.small_strain)
+    oh = ocell.add_material(o.MaterialLinearElastic1('hard', 2, 10e9, .33))
+    os_ = ocell.add_material(o.MaterialLinearElastic1('soft', 2, 70e9, .33))
+    gh = mu.material.MaterialLinearElastic1_2d.make(gcell, 'hard', 10e9, .33)
+    gs = mu.material.MaterialLinearElastic1_2d.make(gcell, 'soft', 70e9, .33)
+    center = np.array([r // 2 for r in res])
+    incl = res[0] // 5
+    for i, pixel in enumerate(gcell):
+        if np.linalg.norm(center - np.array(pixel), 2) < incl:
+            gh.add_pixel(pixel)
+            oh.add_pixel(i)
+        else:
+            gs.add_pixel(pixel)
+            os_.add_pixel(i)
+    return ocell, gcell
+
+
+def test_readme_case_fp64(mu):
+    """The README example (BASELINE config 1): F and P within 1e-10 relative, same
+    Newton and CG iteration counts as the oracle."""
+    ocell, gcell = _readme_pair(mu)
+    Del0 = np.array([[.0, .0], [0, .03]])
+    Del0 = .5 * (Del0 + Del0.T)
+    osol = o.SolverCG(ocell, 1e-8, 401)
+    ro = o.newton_cg(ocell, Del0, osol, 1e-5, 2, 0)
+    gsol = mu.solvers.SolverCG(gcell, 1e-8, 401, verbose=False)
+    rg = mu.solvers.newton_cg(gcell, Del0, gsol, 1e-5, 2)
+    assert (rg.nb_it, rg.nb_fev) == (ro.nb_it, ro.nb_fev)
+    assert rg.success == ro.success and rg.message == ro.message
+    assert rel(rg.grad, ro.grad) < 1e-10
+    assert rel(rg.stress, ro.stress) < 1e-10
+    assert rel(o.homogenised(rg.stress, 2), o.homogenised(ro.stress, 2)) < 1e-10
+
+
+def _spheres_pair(mu, n, form, law='le1', seed=3, nsph=6):
+    rng = np.random.default_rng(seed)
+    res = [n, n, n]
+    ocell = o.Cell(res, [1., 1., 1.], form)
+    gcell = mu.Cell(res, [1., 1., 1.], mu.Formulation(form))
+    grid = np.stack(np.meshgrid(*[np.arange(n)] * 3, indexing='ij'), -1).reshape(-1, 3)
+    inside = np.zeros(n ** 3, dtype=bool)
+    for _ in range(nsph):
+        c = rng.uniform(0, n, 3)
+        r = rng.uniform(n / 10, n / 4)
+        d = np.abs(grid - c)
+        d = np.minimum(d, n - d)
+        inside |= (d ** 2).sum(1) < r * r
+    if law == 'le1':
+        for name, E, mask in (('incl', 210e9, inside), ('matrix', 3e9, ~inside)):
+            om = ocell.add_material(o.MaterialLinearElastic1(name, 3, E, .3))
+            for i in np.flatnonzero(mask):
+                om.add_pixel(i)
+            mu.material.MaterialLinearElastic1_3d.make(gcell, name, E, .3).add_pixels(mask)
+    else:
+        E = np.exp(rng.normal(np.log(1e9), 0.8, n ** 3))
+        nu = rng.uniform(0.2, 0.4, n ** 3)
+        om = ocell.add_material(o.MaterialLinearElastic4('m', 3))
+        for i in range(n ** 3):
+            om.add_pixel(i, E[i], nu[i])
+        mu.material.MaterialLinearElastic4_3d.make(gcell, 'm').add_pixels(np.arange(n ** 3), E, nu)
+    return ocell, gcell
+
+
+def _oracle_variants(build, D, tol, ntol):
+    """The oracle twice: with scipy's and with numpy's FFT.  Their spread is the
+    rounding sensitivity of the method itself on this input (any two FP64
+    implementations, the reference included, differ by about as much)."""
+    import scipy.fft as sfft
+    out = []
+    for lib in (sfft, None):
+        saved = o._sfft
+        o._sfft = lib
+        try:
+            cell = build()
+            out.append(o.newton_cg(cell, D, o.SolverCG(cell, tol, 1000), ntol, 0.0, 0))
+        finally:
+            o._sfft = saved
+    return out
+
+
+@pytest.mark.parametrize('n,form,law,load', [
+    (15, o.FINITE_STRAIN, 'le1', 'uniaxial'),
+    (15, o.SMALL_STRAIN, 'le4', 'shear'),
+    (25, o.FINITE_STRAIN, 'le1', 'uniaxial'),
+])
+def test_newton_cg_3d_fp64(mu, n, form, law, load):
+    """Odd twins of BASELINE configs 2 and 3 (finite-strain LE1 spheres, small-strain
+    lognormal LE4) in FP64.  Criteria: the strain field and the homogenised strain
+    to 1e-10; the same number of Newton steps; CG counts within 1%; the returned
+    stress (evaluated before the last Newton increment, so it carries the CG
+    tolerance) within 1e-10 or 10x the oracle's own FFT-rounding spread, whichever
+    is larger."""
+    ocell, gcell = _spheres_pair(mu, n, form, law)
+    D = np.zeros((3, 3))
+    if load == 'uniaxial':
+        D[0, 0] = 0.02
+    else:
+        D[0, 1] = D[1, 0] = 0.01
+    tol, ntol = 1e-8, 1e-6
+    ro, ro2 = _oracle_variants(lambda: _spheres_pair(mu, n, form, law)[0], D, tol, ntol)
+    gsol = mu.solvers.SolverCG(gcell, tol, 1000)
+    rg = mu.solvers.newton_cg(gcell, D, gsol, ntol, 0.0)
+    assert rg.nb_it == ro.nb_it
+    assert abs(rg.nb_fev - ro.nb_fev) <= max(1, 0.01 * ro.nb_fev)
+    assert rel(rg.grad, ro.grad) < 1e-10
+    assert rel(o.homogenised(rg.grad, 3), o.homogenised(ro.grad, 3)) < 1e-10
+    spread = rel(ro2.stress, ro.stress)
+    assert rel(rg.stress, ro.stress) < max(1e-10, 10 * spread)
+    hspread = rel(o.homogenised(ro2.stress, 3), o.homogenised(ro.stress, 3))
+    assert rel(o.homogenised(rg.stress, 3), o.homogenised(ro.stress, 3)) < max(1e-10, 10 * hspread)
+
+
+def test_mixed_precision_error(mu):
+    """FP32 inner CG with FP64 Newton: homogenised stress within 1e-6 of the FP64
+    oracle."""
+    ocell, gcell = _spheres_pair(mu, 25, o.FINITE_STRAIN, 'le1')
+    D = np.zeros((3, 3))
+    D[0, 0] = 0.02
+    ro = o.newton_cg(ocell, D, o.SolverCG(ocell, 1e-8, 1000), 1e-6, 0.0, 0)
+    rg = mu.solvers.newton_cg(gcell, D, mu.solvers.SolverCG(gcell, 1e-8, 1000, precision='mixed'), 1e-6, 0.0)
+    assert rg.success
+    assert rel(o.homogenised(rg.stress, 3), o.homogenised(ro.stress, 3)) < 1e-6
+
+
+def test_laminate_patch_gpu(mu):
+    """test_solver_newton_cg.cc:218-323 on the GPU: exact layer strains to 1e-12."""
+    res = [3, 3]
+    cell = mu.Cell(res, [1., 1.], mu.Formulation.small_strain)
+    hard = mu.material.MaterialLinearElastic1_2d.make(cell, 'hard', 4.0, .33)
+    soft = mu.material.MaterialLinearElastic1_2d.make(cell, 'soft', 2.0, .33)
+    for pixel in cell:
+        (hard if pixel[0] < 1 else soft).add_pixel(pixel)
+    factor = 1 / 2 * 1 / 3 + 1. - 1 / 3.
+    eps_soft = 1.0 / factor
+    eps_hard = eps_soft / 2
+    for pattern in (np.array([[1., 0], [0, 0]]), np.array([[0, 1.], [1., 0]])):
+        solver = mu.solvers.SolverCG(cell, 1e-8, 20)
+        r = mu.solvers.newton_cg(cell, pattern, solver, 1e-5, 1e-10)
+        F = cell.get_strain()
+        for i, pixel in enumerate(cell):
+            ref = (eps_hard if pixel[0] < 1 else eps_soft) * pattern
+            assert np.linalg.norm(F[:, i].reshape(2, 2).T - ref) <= 1e-12
+        assert r.success
+
+
+def test_le4_homogeneous_gpu(mu):
+    """python_material_linear_elastic4_test.py:63-86."""
+    cell = mu.Cell([7, 7], [2.3, 3.9], mu.Formulation.small_strain)
+    mat = mu.material.MaterialLinearElastic4_2d.make(cell, 'material')
+    for pixel in cell:
+        mat.add_pixel(pixel, 10., 0.3)
+    cell.initialise()
+    Del0 = np.array([[0, 0.025], [0.025, 0]])
+    r = mu.solvers.newton_cg(cell, Del0, mu.solvers.SolverCG(cell, 1e-6, 100, False), 1e-6, 1e-6, False)
+    stress = 2 * (10. / (2 * 1.3)) * Del0
+    assert np.linalg.norm(r.stress.reshape(-1, 4) - stress.reshape(1, 4)) < 1e-8
+
+
+def test_errors(mu):
+    """ConvergenceError (solver_cg.cc:99-108), SolverError for an asymmetric
+    small-strain load (solvers.cc:117-124), coverage errors (cell_base.cc:486-526)."""
+    rng = np.random.default_rng(2)
+    cell = mu.Cell([5, 5], [1., 1.], mu.Formulation.small_strain)
+    m = mu.material.MaterialLinearElastic4_2d.make(cell, 'm')
+    m.add_pixels(np.arange(25), rng.uniform(1, 10, 25), 0.3)
+    with pytest.raises(mu.ConvergenceError):
+        mu.solvers.newton_cg(cell, np.array([[1., 0], [0, 0]]), mu.solvers.SolverCG(cell, 1e-10, 1), 1e-5, 1e-10)
+    with pytest.raises(mu.SolverError):
+        mu.solvers.newton_cg(cell, np.array([[0, 1.], [0, 0]]), mu.solvers.SolverCG(cell, 1e-8, 20), 1e-5, 1e-10)
+    c2 = mu.Cell([3, 3], [1., 1.], mu.Formulation.small_strain)
+    m2 = mu.material.MaterialLinearElastic1_2d.make(c2, 'm', 1., .3)
+    m2.add_pixel([0, 0])
+    with pytest.raises(RuntimeError, match='not assigned'):
+        c2.initialise()
+
+
+def test_hep1_load_steps(mu):
+    """Multi-step finite-strain elasto-plastic solve (state kept on the device between
+    load steps) vs the oracle, on an odd grid with distinct principal stretches."""
+    res = [5, 5, 5]
+    ocell, gcell, rng = _random_cell_pair(mu, res, o.FINITE_STRAIN, 31, laws=('hep1', 'hep1'))
+    steps = []
+    for k in range(1, 4):
+        D = np.zeros((3, 3))
+        D[0, 0], D[1, 1], D[0, 1] = 0.004 * k, -0.0013 * k, 0.0007 * k
+        steps.append(D)
+    try:
+        ro = o.newton_cg(ocell, steps, o.SolverCG(ocell, 1e-8, 500), 1e-6, 0.0, 0)
+    except o.ConvergenceError:
+        with pytest.raises(mu.ConvergenceError):
+            mu.solvers.newton_cg(gcell, steps, mu.solvers.SolverCG(gcell, 1e-8, 500), 1e-6, 0.0)
+        return
+    rg = mu.solvers.newton_cg(gcell, steps, mu.solvers.SolverCG(gcell, 1e-8, 500), 1e-6, 0.0)
+    for a, b in zip(rg, ro):
+        assert (a.nb_it, a.nb_fev) == (b.nb_it, b.nb_fev)
+        assert rel(a.stress, b.stress) < 1e-8
