@@ -57,6 +57,8 @@ def parse():
     ap.add_argument('--e2e-steps', type=int, default=2)
     ap.add_argument('--cpu-cg-iters', type=int, default=4)
     ap.add_argument('--no-cpu', action='store_true')
+    ap.add_argument('--only', default='all', choices=['all', 'mixed'],
+                    help="'mixed': the mixed-precision solves only (for profiler launch lists)")
     return ap.parse_args()
 
 
@@ -274,6 +276,13 @@ def main():
         t_ms = float(t.item())
     value = world * args.steps / (t_ms / 1000.0)
     stress_mixed = None
+
+    if args.only == 'mixed':
+        if rank == 0:
+            print(json.dumps({'metric': 'RVE solves/s (mixed only)', 'value': value, 'unit': 'solves/s',
+                              'ms_per_step': t_ms / args.steps, 'cg_iters_per_solve': cg_per_solve,
+                              'gpu_launches': launches}), flush=True)
+        return
 
     # per-kernel profile of one CG iteration (mixed) + roofline
     prof = mixed.profile(5)
