@@ -183,6 +183,19 @@ int musg_projection_create(int dim, const int *resolutions, const double *length
                            int kind, int flags, musg_projection **out);
 int musg_projection_destroy(musg_projection *proj);
 int musg_projection_apply(musg_projection *proj, double *vec);
+/* Allocation-free variant of musg_projection_apply, for callers that cannot
+ * allocate device memory (a caller-owned pool or arena that forbids cudaMalloc,
+ * allocation-free real-time loops).  No counterpart in the reference.  in_device /
+ * out_device are caller DEVICE buffers of nb_dof doubles in the reference layout
+ * (may be the same buffer); the work is enqueued on cuda_stream and the call
+ * returns before it finishes.  All temporaries live in one 64 MiB file-scope device
+ * array that every GPU loading the library holds until exit; grids that do not fit
+ * are rejected with MUSG_ERR_ARGUMENT.  The first call on a device looks the
+ * array's address up, so make it before any stream capture.  Calls share the
+ * array: calls that overlap on the GPU race and must be serialised by the caller. */
+int musg_projection_apply_noalloc(int dim, const int *resolutions, const double *lengths,
+                                  int kind, int flags, const double *in_device,
+                                  double *out_device, void *cuda_stream);
 /* get_operator(): rows x nb_hermitian doubles, column-major as the reference
  * stores Ghat (rows = D^4 for small/full finite strain, D for the fast variant);
  * out may be NULL to query rows/cols */

@@ -90,6 +90,7 @@ _SIGNATURES = {
     'musg_projection_destroy': (C.c_int, [_P]),
     'musg_projection_apply': (C.c_int, [_P, _D]),
     'musg_projection_get_operator': (C.c_int, [_P, _D, _LL, _LL]),
+    'musg_projection_apply_noalloc': (C.c_int, [C.c_int, _I, _D, C.c_int, C.c_int, _P, _P, _P]),
 }
 
 _lib = None

@@ -1028,6 +1028,13 @@ int musg_projection_create(int dim, const int *resolutions, const double *length
   });
 }
 
+int musg_projection_apply_noalloc(int dim, const int *resolutions, const double *lengths, int kind, int flags,
+                                  const double *in_device, double *out_device, void *cuda_stream) {
+  return guard([&] {
+    noalloc_project(dim, resolutions, lengths, kind, flags, in_device, out_device, (cudaStream_t)cuda_stream);
+  });
+}
+
 int musg_projection_destroy(musg_projection *proj) {
   return guard([&] { delete proj; });
 }

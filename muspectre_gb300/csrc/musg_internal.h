@@ -219,6 +219,10 @@ void soa_to_aos(const double *soa, double *aos, int ncomp, long long npx, cudaSt
 void soa_to_aos_complex(const double2 *soa, double2 *aos, int ncomp, long long nk, cudaStream_t s);
 void aos_to_soa_complex(const double2 *aos, double2 *soa, int ncomp, long long nk, cudaStream_t s);
 
+// allocation-free projection on caller device buffers (noalloc.cu)
+void noalloc_project(int dim, const int *resolutions, const double *lengths, int kind, int flags,
+                     const double *in_device, double *out_device, cudaStream_t s);
+
 // simple device buffer
 struct DevBuf {
   void *p = nullptr;
