@@ -357,6 +357,7 @@ def main():
         'roofline': roof,
         'clocks': clocks,
         'gpu_launches': launches,
+        'launch_shapes': cell.tuning(),
         'e2e': {'value': e2e_v, 'unit': 'solves/s', 'h2d_bytes_per_step': h2d, 'd2h_bytes_per_step': d2h},
     }
     if rank == 0 and not args.no_cpu:

@@ -114,6 +114,11 @@ int musg_material_size(musg_cell *cell, int material, long long *count);
  * upload of the microstructure, FFT plans.  Called implicitly by the first
  * evaluation. plan_flags follows FFT_PlanFlags (estimate=0, measure=1, patient=2). */
 int musg_cell_initialise(musg_cell *cell, int plan_flags);
+/* launch shapes of the spectral passes (threads per block, shared-memory target
+ * per block) for FP64 then FP32, passes last-axis / middle-axis / Green: 6 entries
+ * each.  FFT_PlanFlags measure/patient at initialise times candidates on the cell's
+ * grid (the FFTW_MEASURE analogue); no counterpart in the reference. */
+int musg_cell_tuning(musg_cell *cell, int *threads, long long *bytes);
 /* CellBase::set_uniform_strain (cell_base.cc:110-112); strain is D*D column-major */
 int musg_cell_set_uniform_strain(musg_cell *cell, const double *strain);
 /* Cell::get_strain_vector / get_stress_vector (cell_base.cc:96-106): copies */

@@ -62,6 +62,7 @@ _SIGNATURES = {
     'musg_material_add_pixels': (C.c_int, [_P, C.c_int, _LL, C.c_longlong, _D, C.c_int]),
     'musg_material_size': (C.c_int, [_P, C.c_int, _LL]),
     'musg_cell_initialise': (C.c_int, [_P, C.c_int]),
+    'musg_cell_tuning': (C.c_int, [_P, _I, _LL]),
     'musg_cell_set_uniform_strain': (C.c_int, [_P, _D]),
     'musg_cell_get_strain': (C.c_int, [_P, _D]),
     'musg_cell_set_strain': (C.c_int, [_P, _D]),

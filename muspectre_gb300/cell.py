@@ -165,6 +165,15 @@ class CellBase:
     def _to_array(self, flat):
         return flat.reshape(self.nb_pixels, self.dim * self.dim).T
 
+    def tuning(self):
+        """Launch shapes of the spectral passes {precision: {pass: (threads, smem bytes)}}."""
+        t = np.zeros(6, dtype=np.int32)
+        b = np.zeros(6, dtype=np.int64)
+        L.check(L.lib().musg_cell_tuning(self._h, L.iptr(t), L.llptr(b)))
+        names = ('last_axis', 'middle_axis', 'green')
+        return {prec: {names[k]: (int(t[3 * p + k]), int(b[3 * p + k])) for k in range(3)}
+                for p, prec in enumerate(('fp64', 'fp32'))}
+
     def set_uniform_strain(self, strain):
         """CellBase::set_uniform_strain (cell_base.cc:110-112)."""
         m = np.asarray(strain, dtype=np.float64).reshape(self.dim, self.dim)

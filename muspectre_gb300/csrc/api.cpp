@@ -6,7 +6,9 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <memory>
+#include <mutex>
 #include <sstream>
 #include <string>
 #include <vector>
@@ -57,6 +59,46 @@ std::string ccoord_str(const int *res, int dim, long long idx) {
   return o.str();
 }
 
+// Launch shapes found by the autotuner, shared by every cell of the same grid,
+// component count and projection in this process (cf. FFTW wisdom).
+struct Wisdom {
+  int threads[3];
+  long bytes[3];
+};
+std::mutex g_wisdom_mu;
+std::map<std::string, Wisdom> g_wisdom;
+
+std::string wisdom_key(const Spectral &sp, int prec) {
+  std::ostringstream k;
+  k << sp.g.dim << ':' << sp.g.n[0] << 'x' << sp.g.n[1] << 'x' << sp.g.n[2] << ':' << sp.ncomp << ':'
+    << sp.proj_kind << ':' << sp.allow_even << ':' << prec;
+  return k.str();
+}
+
+template <typename R> void autotune_with_wisdom(Spectral &sp, cudaStream_t s, int effort) {
+  const int pi = sizeof(R) == 8 ? 0 : 1;
+  const std::string key = wisdom_key(sp, pi);
+  {
+    std::lock_guard<std::mutex> lock(g_wisdom_mu);
+    auto it = g_wisdom.find(key);
+    if (it != g_wisdom.end()) {
+      for (int k = 0; k < 3; ++k) {
+        sp.tune_threads[pi][k] = it->second.threads[k];
+        sp.tune_bytes[pi][k] = it->second.bytes[k];
+      }
+      return;
+    }
+  }
+  spectral_autotune<R>(sp, s, effort);
+  Wisdom w;
+  for (int k = 0; k < 3; ++k) {
+    w.threads[k] = sp.tune_threads[pi][k];
+    w.bytes[k] = sp.tune_bytes[pi][k];
+  }
+  std::lock_guard<std::mutex> lock(g_wisdom_mu);
+  g_wisdom[key] = w;
+}
+
 struct Material {
   int law = 0;
   std::string name;
@@ -78,6 +120,8 @@ struct musg_cell {
   bool initialised = false;
   bool tangent_valid = false;
   bool need32 = false;
+  int plan_flags = 0;      // FFT_PlanFlags: estimate 0, measure 1, patient 2
+  bool tuned64 = false, tuned32 = false;
   cudaStream_t stream = nullptr;
   bool own_stream = false;
   std::vector<Material> materials;
@@ -265,8 +309,23 @@ struct musg_cell {
       Kp64.alloc((size_t)npx * D2 * dim * sizeof(double));
     }
     if (need32) alloc32();
-    MUSG_CUDA(cudaStreamSynchronize(stream));
     initialised = true;
+    autotune();
+    MUSG_CUDA(cudaStreamSynchronize(stream));
+  }
+
+  // FFT_PlanFlags::measure / patient: time the launch shapes of the passes on this
+  // grid (the analogue of FFTW planning with FFTW_MEASURE)
+  void autotune() {
+    if (plan_flags < 1 || !initialised) return;
+    if (!tuned64) {
+      autotune_with_wisdom<double>(sp, stream, plan_flags);
+      tuned64 = true;
+    }
+    if (need32 && !tuned32) {
+      autotune_with_wisdom<float>(sp, stream, plan_flags);
+      tuned32 = true;
+    }
   }
 
   void alloc32() {
@@ -285,6 +344,7 @@ struct musg_cell {
       if (has_hep && !Kp32.p) Kp32.alloc((size_t)npx * D2 * dim * sizeof(float));
     }
     tangent_valid = false;
+    autotune();
   }
 
   void evaluate(bool want_K) {
@@ -798,7 +858,19 @@ int musg_cell_initialise(musg_cell *cell, int plan_flags) {
   return guard([&] {
     require(cell, MUSG_ERR_ARGUMENT, "null cell");
     require(plan_flags >= 0 && plan_flags <= 2, MUSG_ERR_ARGUMENT, "unknown planner flag type");
+    cell->plan_flags = plan_flags;
     cell->initialise();
+  });
+}
+
+int musg_cell_tuning(musg_cell *cell, int *threads, long long *bytes) {
+  return guard([&] {
+    require(cell && threads && bytes, MUSG_ERR_ARGUMENT, "null argument");
+    for (int p = 0; p < 2; ++p)
+      for (int k = 0; k < 3; ++k) {
+        threads[3 * p + k] = cell->sp.tune_threads[p][k];
+        bytes[3 * p + k] = cell->sp.tune_bytes[p][k];
+      }
   });
 }
 

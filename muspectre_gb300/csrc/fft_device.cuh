@@ -25,6 +25,33 @@
 
 namespace musg {
 
+// Exact division of small non-negative integers by a runtime divisor without the
+// integer-division instruction sequence: q0 = trunc(n * rcp(d)) in FP32 is within one
+// of n/d for 0 <= n < 2^22 (the relative error of the product is below 2^-23 and
+// n/d < 2^22), and one remainder correction makes it exact.
+struct FDiv {
+  int d;
+  float inv;
+  // IEEE division (no fast-math): the correctly rounded reciprocal
+  __device__ __forceinline__ explicit FDiv(int d_) : d(d_), inv(1.0f / (float)d_) {}
+  __device__ __forceinline__ int div(int n, int &r) const {
+    int q = __float2int_rz(__int2float_rn(n) * inv);
+    r = n - q * d;
+    if (r < 0) {
+      q -= 1;
+      r += d;
+    } else if (r >= d) {
+      q += 1;
+      r -= d;
+    }
+    return q;
+  }
+  __device__ __forceinline__ int div(int n) const {
+    int r;
+    return div(n, r);
+  }
+};
+
 template <typename T> __device__ __forceinline__ T cadd(T a, T b) { return T{a.x + b.x, a.y + b.y}; }
 template <typename T> __device__ __forceinline__ T csub(T a, T b) { return T{a.x - b.x, a.y - b.y}; }
 template <typename T> __device__ __forceinline__ T cmul(T a, T b) {
@@ -175,10 +202,11 @@ __device__ __forceinline__ void fft_stage(const typename V2<R>::T *__restrict__ 
   const int nb = m / RAD;
   const int total = nb * P;
   const int tws = m / (Ns * RAD);
+  const FDiv fP(P), fNs(Ns);
   for (int t = threadIdx.x; t < total; t += blockDim.x) {
-    const int j = t / P;
-    const int p = t - j * P;
-    const int k = j % Ns;
+    int p, k;
+    const int j = fP.div(t, p);
+    fNs.div(j, k);
     T v[RAD];
 #pragma unroll
     for (int r = 0; r < RAD; ++r) v[r] = src[(j + r * nb) * P + p];
@@ -235,9 +263,10 @@ __device__ __forceinline__ typename V2<R>::T *fft_run(typename V2<R>::T *a, type
   if (!ap.blu) return fft_stages<R, INV>(a, b, P, ap);
   const int n = ap.n, m = ap.m;
   const int tot = m * P;
+  const FDiv fP(P);
   // x . w (conj(x) for the inverse: IDFT(x) = conj(DFT(conj x))), zero padded
   for (int i = threadIdx.x; i < tot; i += blockDim.x) {
-    const int e = i / P;
+    const int e = fP.div(i);
     if (e < n) {
       T x = a[i];
       if (INV) x.y = -x.y;
@@ -249,11 +278,11 @@ __device__ __forceinline__ typename V2<R>::T *fft_run(typename V2<R>::T *a, type
   __syncthreads();
   T *c = fft_stages<R, false>(a, b, P, ap);
   T *d = (c == a) ? b : a;
-  for (int i = threadIdx.x; i < tot; i += blockDim.x) c[i] = cmul(c[i], __ldg(&ap.bf[i / P]));
+  for (int i = threadIdx.x; i < tot; i += blockDim.x) c[i] = cmul(c[i], __ldg(&ap.bf[fP.div(i)]));
   __syncthreads();
   c = fft_stages<R, true>(c, d, P, ap);
   for (int i = threadIdx.x; i < n * P; i += blockDim.x) {
-    T x = cmul(c[i], __ldg(&ap.chirp[i / P]));
+    T x = cmul(c[i], __ldg(&ap.chirp[fP.div(i)]));
     if (INV) x.y = -x.y;
     c[i] = x;
   }

@@ -129,6 +129,11 @@ struct Spectral {
   void *spec64 = nullptr;   // [ncomp][nk] complex double
   void *spec32 = nullptr;   // [ncomp][nk] complex float
   bool want32 = false;
+  // launch shapes per precision (0: FP64, 1: FP32) and pass (0: last, 1: axis,
+  // 2: green): threads per block and the shared memory a block aims for; set by
+  // the defaults below or by spectral_autotune
+  int tune_threads[2][3] = {{256, 256, 256}, {256, 256, 256}};
+  long tune_bytes[2][3] = {{73728, 49152, 73728}, {73728, 49152, 73728}};
   void init(int dim, const int *res, int ncomp, int proj_kind, const double *lengths,
             bool allow_even, bool want32);
   void ensure32();
@@ -162,6 +167,9 @@ template <typename R>
 void tangent_operator(Spectral &sp, int tkind, const TangentData<R> &td, const R *in,
                       R *out, cudaStream_t s);
 int cg_operator_partials(const Spectral &sp);
+// Times candidate launch shapes of each pass on this grid (CUDA events) and keeps
+// the fastest (FFT_PlanFlags::measure / patient); fp32 selects the FP32 passes.
+template <typename R> void spectral_autotune(Spectral &sp, cudaStream_t s, int effort);
 
 // ---------------------------------------------------------------- CG kernels (cg.cu)
 int reduce_blocks(long long n);

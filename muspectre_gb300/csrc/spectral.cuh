@@ -28,6 +28,9 @@ enum Prologue : int { PRO_PLAIN = 0, PRO_TANGENT = 1, PRO_CG = 2 };
 enum Epilogue : int { EPI_PLAIN = 0, EPI_CG = 1 };
 enum GreenMode : int { GM_SMALL = 0, GM_FINITE = 1, GM_FWD = 2, GM_INV = 3 };
 
+// independent global loads each thread keeps in flight in the staging loops
+constexpr int kLoadBatch = 8;
+
 // ------------------------------------------------------------ reductions
 template <typename R> struct Acc {
   R s = R(0), c = R(0);
@@ -133,28 +136,53 @@ __device__ __forceinline__ void tangent_kprime(const R *dF, const R *Kp, R *out)
   }
 }
 
-template <int D, int TK, typename R>
-__device__ __forceinline__ void apply_tangent(const TangentData<R> &td, long long px, long long npx,
-                                              const R *in, R *out) {
-  constexpr int D2 = D * D;
-  int kind = TK;
-  if constexpr (TK == TK_MIXED) kind = td.law_kind[td.mat[px]];
-  if constexpr (TK == TK_SMALL) {
-    tangent_small<D, R>(in, td.lam[px], td.mu[px], out);
-  } else if (kind == TK_FINITE) {
-    R F[D2], S[D2];
+// Tangent data of one pixel, loaded into registers before anything is stored so that
+// all of a pixel's global loads are in flight together.
+template <int D, int TK, typename R> struct TangentLocal {
+  static constexpr int D2 = D * D;
+  static constexpr bool kFinite = (TK == TK_FINITE || TK == TK_MIXED);
+  static constexpr bool kKprime = (TK == TK_KPRIME || TK == TK_MIXED);
+  int kind;
+  R lam, mu;
+  R F[kFinite ? D2 : 1], S[kFinite ? D2 : 1];
+  R Kp[kKprime ? D2 * D : 1];
+
+  __device__ __forceinline__ void load(const TangentData<R> &td, long long px, long long npx) {
+    kind = TK;
+    if constexpr (TK == TK_MIXED) kind = td.law_kind[td.mat[px]];
+    if constexpr (TK == TK_SMALL || kFinite) {
+      lam = td.lam[px];
+      mu = td.mu[px];
+    }
+    if constexpr (kFinite) {
+      if (TK == TK_FINITE || kind == TK_FINITE) {
 #pragma unroll
-    for (int c = 0; c < D2; ++c) F[c] = td.F[c * npx + px];
+        for (int c = 0; c < D2; ++c) F[c] = td.F[c * npx + px];
 #pragma unroll
-    for (int c = 0; c < D2; ++c) S[c] = td.S[c * npx + px];
-    tangent_finite<D, R>(in, F, S, td.lam[px], td.mu[px], out);
-  } else {
-    R Kp[D2 * D];
+        for (int c = 0; c < D2; ++c) S[c] = td.S[c * npx + px];
+      }
+    }
+    if constexpr (kKprime) {
+      if (TK == TK_KPRIME || kind == TK_KPRIME) {
 #pragma unroll
-    for (int c = 0; c < D2 * D; ++c) Kp[c] = td.Kp[c * npx + px];
-    tangent_kprime<D, R>(in, Kp, out);
+        for (int c = 0; c < D2 * D; ++c) Kp[c] = td.Kp[c * npx + px];
+      }
+    }
   }
-}
+
+  __device__ __forceinline__ void apply(const R *in, R *out) const {
+    if constexpr (TK == TK_SMALL) {
+      tangent_small<D, R>(in, lam, mu, out);
+    } else if constexpr (TK == TK_FINITE) {
+      tangent_finite<D, R>(in, F, S, lam, mu, out);
+    } else if constexpr (TK == TK_KPRIME) {
+      tangent_kprime<D, R>(in, Kp, out);
+    } else {
+      if (kind == TK_FINITE) tangent_finite<D, R>(in, F, S, lam, mu, out);
+      else tangent_kprime<D, R>(in, Kp, out);
+    }
+  }
+};
 
 // ------------------------------------------------------------ pass "last"
 template <typename R> struct LastArgs {
@@ -186,41 +214,63 @@ __global__ void __launch_bounds__(kPassThreads) k_last_fwd(const LastArgs<R> a) 
   T *buf2 = buf + (size_t)P * a.ap.m;
   const long long row0 = (long long)blockIdx.x * G;
   R *bufr = reinterpret_cast<R *>(buf);
+  const FDiv fGL(G * L), fL(L);
   if constexpr (PRO == PRO_PLAIN) {
-    for (int idx = threadIdx.x; idx < nc * G * L; idx += blockDim.x) {
-      const int c = idx / (G * L);
-      const int rem = idx - c * G * L;
-      const int g = rem / L, e = rem - g * L;
-      const long long row = row0 + g;
-      R v = R(0);
-      if (row < a.nrows) v = a.in[(long long)c * a.npx + row * L + e] * a.scale;
-      bufr[2 * (e * P + c * G2 + (g >> 1)) + (g & 1)] = v;
+    const int total = nc * G * L;
+    for (int i0 = threadIdx.x; i0 < total; i0 += kLoadBatch * blockDim.x) {
+      R v[kLoadBatch];
+      int dst[kLoadBatch];
+#pragma unroll
+      for (int u = 0; u < kLoadBatch; ++u) {
+        const int idx = i0 + u * blockDim.x;
+        dst[u] = -1;
+        v[u] = R(0);
+        if (idx < total) {
+          int rem, e;
+          const int c = fGL.div(idx, rem);
+          const int g = fL.div(rem, e);
+          const long long row = row0 + g;
+          if (row < a.nrows) v[u] = a.in[(long long)c * a.npx + row * L + e];
+          dst[u] = 2 * (e * P + c * G2 + (g >> 1)) + (g & 1);
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < kLoadBatch; ++u)
+        if (dst[u] >= 0) bufr[dst[u]] = v[u] * a.scale;
     }
   } else {
     constexpr int D2 = D * D;
     const bool first = (PRO == PRO_CG) ? (a.st->iter == 0) : false;
     const R beta = (PRO == PRO_CG) ? R(a.st->beta) : R(0);
     for (int idx = threadIdx.x; idx < G * L; idx += blockDim.x) {
-      const int g = idx / L, e = idx - g * L;
+      int e;
+      const int g = fL.div(idx, e);
       const long long row = row0 + g;
       R out[D2];
       if (row < a.nrows) {
         const long long px = row * L + e;
         R v[D2];
+        TangentLocal<D, TK, R> tl;
         if (PRO == PRO_CG) {
+          R rv[D2], pv[D2];
 #pragma unroll
           for (int c = 0; c < D2; ++c) {
             const long long o = (long long)c * a.npx + px;
-            R pv = -a.r[o];
-            if (!first) pv += beta * a.p[o];
-            a.p[o] = pv;
-            v[c] = pv;
+            rv[c] = a.r[o];
+            pv[c] = first ? R(0) : a.p[o];
+          }
+          tl.load(a.td, px, a.npx);
+#pragma unroll
+          for (int c = 0; c < D2; ++c) {
+            v[c] = first ? -rv[c] : -rv[c] + beta * pv[c];
+            a.p[(long long)c * a.npx + px] = v[c];
           }
         } else {
 #pragma unroll
           for (int c = 0; c < D2; ++c) v[c] = a.in[(long long)c * a.npx + px];
+          tl.load(a.td, px, a.npx);
         }
-        apply_tangent<D, TK, R>(a.td, px, a.npx, v, out);
+        tl.apply(v, out);
       } else {
 #pragma unroll
         for (int c = 0; c < D2; ++c) out[c] = R(0);
@@ -233,10 +283,11 @@ __global__ void __launch_bounds__(kPassThreads) k_last_fwd(const LastArgs<R> a) 
   const T *res = fft_run<R, false>(buf, buf2, P, a.ap);
   // unpack the two real spectra: X = (Z_k + conj Z_{L-k})/2, Y = -i (Z_k - conj Z_{L-k})/2
   const int H = a.H;
+  const FDiv fGH(G * H), fH(H);
   for (int idx = threadIdx.x; idx < nc * G * H; idx += blockDim.x) {
-    const int c = idx / (G * H);
-    const int rem = idx - c * G * H;
-    const int gr = rem / H, k = rem - gr * H;
+    int rem, k;
+    const int c = fGH.div(idx, rem);
+    const int gr = fH.div(rem, k);
     const long long row = row0 + gr;
     if (row >= a.nrows) continue;
     const int q = c * G2 + (gr >> 1);
@@ -262,27 +313,46 @@ __global__ void __launch_bounds__(kPassThreads) k_last_inv(const LastArgs<R> a) 
   T *buf2 = buf + (size_t)P * a.ap.m;
   const long long row0 = (long long)blockIdx.x * G;
   const bool even = (L & 1) == 0;
-  for (int idx = threadIdx.x; idx < nc * G2 * H; idx += blockDim.x) {
-    const int c = idx / (G2 * H);
-    const int rem = idx - c * G2 * H;
-    const int g2 = rem / H, k = rem - g2 * H;
-    const long long rx = row0 + 2 * g2, ry = rx + 1;
-    T X = T{R(0), R(0)}, Y = T{R(0), R(0)};
-    if (rx < a.nrows) X = a.spec[(long long)c * a.nk + rx * H + k];
-    if (ry < a.nrows) Y = a.spec[(long long)c * a.nk + ry * H + k];
-    const bool selfconj = (k == 0) || (even && 2 * k == L);
-    if (selfconj) { X.y = R(0); Y.y = R(0); }  // c2r uses the real part only
-    const int q = c * G2 + g2;
-    buf[k * P + q] = T{X.x - Y.y, X.y + Y.x};
-    if (!selfconj) buf[(L - k) * P + q] = T{X.x + Y.y, Y.x - X.y};
+  const int total = nc * G2 * H;
+  const FDiv fG2H(G2 * H), fH(H), fGL(G * L), fL(L);
+  for (int i0 = threadIdx.x; i0 < total; i0 += kLoadBatch * blockDim.x) {
+    T X[kLoadBatch], Y[kLoadBatch];
+#pragma unroll
+    for (int u = 0; u < kLoadBatch; ++u) {
+      const int idx = i0 + u * blockDim.x;
+      X[u] = T{R(0), R(0)};
+      Y[u] = T{R(0), R(0)};
+      if (idx < total) {
+        int rem, k;
+        const int c = fG2H.div(idx, rem);
+        const int g2 = fH.div(rem, k);
+        const long long rx = row0 + 2 * g2, ry = rx + 1;
+        if (rx < a.nrows) X[u] = a.spec[(long long)c * a.nk + rx * H + k];
+        if (ry < a.nrows) Y[u] = a.spec[(long long)c * a.nk + ry * H + k];
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < kLoadBatch; ++u) {
+      const int idx = i0 + u * blockDim.x;
+      if (idx >= total) continue;
+      int rem, k;
+      const int c = fG2H.div(idx, rem);
+      const int g2 = fH.div(rem, k);
+      T x = X[u], y = Y[u];
+      const bool selfconj = (k == 0) || (even && 2 * k == L);
+      if (selfconj) { x.y = R(0); y.y = R(0); }  // c2r uses the real part only
+      const int q = c * G2 + g2;
+      buf[k * P + q] = T{x.x - y.y, x.y + y.x};
+      if (!selfconj) buf[(L - k) * P + q] = T{x.x + y.y, y.x - x.y};
+    }
   }
   __syncthreads();
   const R *bufr = reinterpret_cast<const R *>(fft_run<R, true>(buf, buf2, P, a.ap));
   if constexpr (EPI == EPI_PLAIN) {
     for (int idx = threadIdx.x; idx < nc * G * L; idx += blockDim.x) {
-      const int c = idx / (G * L);
-      const int rem = idx - c * G * L;
-      const int g = rem / L, e = rem - g * L;
+      int rem, e;
+      const int c = fGL.div(idx, rem);
+      const int g = fL.div(rem, e);
       const long long row = row0 + g;
       if (row < a.nrows) a.out[(long long)c * a.npx + row * L + e] = a.scale * bufr[2 * (e * P + c * G2 + (g >> 1)) + (g & 1)];
     }
@@ -290,7 +360,8 @@ __global__ void __launch_bounds__(kPassThreads) k_last_inv(const LastArgs<R> a) 
     constexpr int D2 = D * D;
     Acc<R> acc;
     for (int idx = threadIdx.x; idx < G * L; idx += blockDim.x) {
-      const int g = idx / L, e = idx - g * L;
+      int e;
+      const int g = fL.div(idx, e);
       const long long row = row0 + g;
       if (row >= a.nrows) continue;
       const long long px = row * L + e;
@@ -328,15 +399,32 @@ __global__ void __launch_bounds__(kPassThreads) k_axis(const AxisArgs<R> a) {
   T *buf2 = buf + (size_t)Tt * a.ap.m;
   T *base = a.spec + batch * a.sb;
   const long long pos0 = (long long)tile * Tt;
-  for (int idx = threadIdx.x; idx < a.nax * Tt; idx += blockDim.x) {
-    const int e = idx / Tt, t = idx - e * Tt;
-    const long long pos = pos0 + t;
-    buf[idx] = (pos < a.inner) ? base[e * a.se + pos] : T{R(0), R(0)};
+  const int total = a.nax * Tt;
+  const FDiv fT(Tt);
+  for (int i0 = threadIdx.x; i0 < total; i0 += kLoadBatch * blockDim.x) {
+    T v[kLoadBatch];
+#pragma unroll
+    for (int u = 0; u < kLoadBatch; ++u) {
+      const int idx = i0 + u * blockDim.x;
+      v[u] = T{R(0), R(0)};
+      if (idx < total) {
+        int t;
+        const int e = fT.div(idx, t);
+        const long long pos = pos0 + t;
+        if (pos < a.inner) v[u] = base[e * a.se + pos];
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < kLoadBatch; ++u) {
+      const int idx = i0 + u * blockDim.x;
+      if (idx < total) buf[idx] = v[u];
+    }
   }
   __syncthreads();
   const T *res = fft_run<R, INV>(buf, buf2, Tt, a.ap);
   for (int idx = threadIdx.x; idx < a.nax * Tt; idx += blockDim.x) {
-    const int e = idx / Tt, t = idx - e * Tt;
+    int t;
+    const int e = fT.div(idx, t);
     const long long pos = pos0 + t;
     if (pos < a.inner) base[e * a.se + pos] = res[idx];
   }
@@ -364,26 +452,43 @@ __global__ void __launch_bounds__(kPassThreads) k_green(const GreenArgs<R> a) {
   const int P = nc * Tt;
   T *buf2 = buf + (size_t)P * a.ap.m;
   const long long rho0 = (long long)blockIdx.x * Tt;
-  for (int idx = threadIdx.x; idx < nc * n0 * Tt; idx += blockDim.x) {
-    const int t = idx % Tt;
-    const int rest = idx / Tt;
-    const int e = rest % n0, c = rest / n0;
-    const long long rho = rho0 + t;
-    buf[e * P + c * Tt + t] = (rho < a.Rr) ? a.spec[(long long)c * a.nk + e * a.Rr + rho] : T{R(0), R(0)};
+  const int total = nc * n0 * Tt;
+  const FDiv fT(Tt), fn0(n0);
+  for (int i0 = threadIdx.x; i0 < total; i0 += kLoadBatch * blockDim.x) {
+    T v[kLoadBatch];
+    int dst[kLoadBatch];
+#pragma unroll
+    for (int u = 0; u < kLoadBatch; ++u) {
+      const int idx = i0 + u * blockDim.x;
+      v[u] = T{R(0), R(0)};
+      dst[u] = -1;
+      if (idx < total) {
+        int t, e;
+        const int rest = fT.div(idx, t);
+        const int c = fn0.div(rest, e);
+        const long long rho = rho0 + t;
+        if (rho < a.Rr) v[u] = a.spec[(long long)c * a.nk + e * a.Rr + rho];
+        dst[u] = e * P + c * Tt + t;
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < kLoadBatch; ++u)
+      if (dst[u] >= 0) buf[dst[u]] = v[u];
   }
   __syncthreads();
   T *cur = buf;
   if (MODE != GM_INV) cur = fft_run<R, false>(buf, buf2, P, a.ap);
   if constexpr (MODE == GM_SMALL || MODE == GM_FINITE) {
     constexpr int D2 = D * D;
+    const FDiv fnh(a.nh);
     for (int idx = threadIdx.x; idx < n0 * Tt; idx += blockDim.x) {
-      const int e = idx / Tt, t = idx - e * Tt;
+      int t;
+      const int e = fT.div(idx, t);
       const long long rho = rho0 + t;
       if (rho >= a.Rr) continue;
       int k1, k2 = 0;
       if (D == 3) {
-        k1 = (int)(rho / a.nh);
-        k2 = (int)(rho - (long long)k1 * a.nh);
+        k1 = fnh.div((int)rho, k2);
       } else {
         k1 = (int)rho;
       }
@@ -453,9 +558,9 @@ __global__ void __launch_bounds__(kPassThreads) k_green(const GreenArgs<R> a) {
   }
   if (MODE != GM_FWD) cur = fft_run<R, true>(cur, cur == buf ? buf2 : buf, P, a.ap);
   for (int idx = threadIdx.x; idx < nc * n0 * Tt; idx += blockDim.x) {
-    const int t = idx % Tt;
-    const int rest = idx / Tt;
-    const int e = rest % n0, c = rest / n0;
+    int t, e;
+    const int rest = fT.div(idx, t);
+    const int c = fn0.div(rest, e);
     const long long rho = rho0 + t;
     if (rho < a.Rr) a.spec[(long long)c * a.nk + e * a.Rr + rho] = cur[e * P + c * Tt + t];
   }

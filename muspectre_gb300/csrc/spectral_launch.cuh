@@ -35,22 +35,22 @@ template <typename K> void allow_smem(K kernel) {
   done.insert(key);
 }
 
-// complex elements per block the configurations aim for (latency hiding vs. the
-// number of blocks)
-constexpr long kTargetElems = 8192;
-
 struct Cfg {
   int per;       // rows per block (last pass) or tile (axis / green passes)
   int blocks;
   size_t smem;
+  int threads;
 };
+
+template <typename R> constexpr int prec_index() { return sizeof(R) == 8 ? 0 : 1; }
 
 // shared memory per block: two ping-pong buffers of (pencils x m) complex values
 template <typename R> Cfg last_cfg(const Spectral &sp) {
   const AxisPlan &ap = sp.ax[sp.g.dim - 1];
   const long per_pair = (long)sp.ncomp * ap.m;
   const long eb = 2 * sizeof(typename V2<R>::T);
-  long g2 = std::min(kTargetElems / per_pair, (long)optin_smem() / (per_pair * eb));
+  const long target = sp.tune_bytes[prec_index<R>()][0];
+  long g2 = std::min(std::max(1L, target / (per_pair * eb)), (long)optin_smem() / (per_pair * eb));
   if (g2 < 1) throw Error(MUSG_ERR_ARGUMENT, "last-axis FFT too long for one thread block");
   g2 = std::min<long>(g2, 16);
   g2 = std::min<long>(g2, (sp.g.nrows + 1) / 2);
@@ -58,22 +58,27 @@ template <typename R> Cfg last_cfg(const Spectral &sp) {
   c.per = (int)(2 * g2);
   c.blocks = (int)((sp.g.nrows + c.per - 1) / c.per);
   c.smem = (size_t)(g2 * per_pair * eb);
+  c.threads = sp.tune_threads[prec_index<R>()][0];
   return c;
 }
 
 template <typename R> Cfg axis_cfg(const Spectral &sp, int axis, long long inner, long long nbatch) {
   const AxisPlan &ap = sp.ax[axis];
   const long eb = 2 * sizeof(typename V2<R>::T);
-  long T = std::min(kTargetElems / ap.m, (long)optin_smem() / (ap.m * eb));
+  const long target = sp.tune_bytes[prec_index<R>()][1];
+  long T = std::min(std::max(1L, target / (ap.m * eb)), (long)optin_smem() / (ap.m * eb));
   if (T < 1) throw Error(MUSG_ERR_ARGUMENT, "FFT axis too long for one thread block");
   T = std::min<long>(T, 32);
-  if (T > 8) T &= ~3L;
   T = std::min<long>(T, inner);
+  // balance the tiles over the inner extent (65 -> 22 + 22 + 21, not 32 + 32 + 1)
+  const long nt = (inner + T - 1) / T;
+  T = (inner + nt - 1) / nt;
   Cfg c;
   c.per = (int)T;
   const long long ntiles = (inner + T - 1) / T;
   c.blocks = (int)(ntiles * nbatch);
   c.smem = (size_t)(T * ap.m * eb);
+  c.threads = sp.tune_threads[prec_index<R>()][1];
   return c;
 }
 
@@ -81,15 +86,16 @@ template <typename R> Cfg green_cfg(const Spectral &sp, long long Rr) {
   const AxisPlan &ap = sp.ax[0];
   const long per = (long)sp.ncomp * ap.m;
   const long eb = 2 * sizeof(typename V2<R>::T);
-  long T = std::min(kTargetElems / per, (long)optin_smem() / (per * eb));
+  const long target = sp.tune_bytes[prec_index<R>()][2];
+  long T = std::min(std::max(1L, target / (per * eb)), (long)optin_smem() / (per * eb));
   if (T < 1) throw Error(MUSG_ERR_ARGUMENT, "first-axis FFT too long for one thread block");
   T = std::min<long>(T, 32);
-  if (T > 8) T &= ~3L;
   T = std::min<long>(T, Rr);
   Cfg c;
   c.per = (int)T;
   c.blocks = (int)((Rr + T - 1) / T);
   c.smem = (size_t)(T * per * eb);
+  c.threads = sp.tune_threads[prec_index<R>()][2];
   return c;
 }
 
@@ -121,7 +127,7 @@ template <typename R, int PRO, int D, int TK>
 void launch_fwd(const LastArgs<R> &a, const Cfg &c, cudaStream_t s) {
   auto k = k_last_fwd<R, PRO, D, TK>;
   allow_smem(k);
-  k<<<c.blocks, kPassThreads, c.smem, s>>>(a);
+  k<<<c.blocks, c.threads, c.smem, s>>>(a);
   MUSG_CHECK_LAUNCH();
 }
 
@@ -143,7 +149,7 @@ template <typename R, int EPI, int D>
 void launch_inv(const LastArgs<R> &a, const Cfg &c, cudaStream_t s) {
   auto k = k_last_inv<R, EPI, D>;
   allow_smem(k);
-  k<<<c.blocks, kPassThreads, c.smem, s>>>(a);
+  k<<<c.blocks, c.threads, c.smem, s>>>(a);
   MUSG_CHECK_LAUNCH();
 }
 
@@ -166,11 +172,11 @@ void run_axis(Spectral &sp, bool inv, const CGState *st, cudaStream_t s) {
   if (inv) {
     auto k = k_axis<R, true>;
     allow_smem(k);
-    k<<<c.blocks, kPassThreads, c.smem, s>>>(a);
+    k<<<c.blocks, c.threads, c.smem, s>>>(a);
   } else {
     auto k = k_axis<R, false>;
     allow_smem(k);
-    k<<<c.blocks, kPassThreads, c.smem, s>>>(a);
+    k<<<c.blocks, c.threads, c.smem, s>>>(a);
   }
   MUSG_CHECK_LAUNCH();
 }
@@ -203,7 +209,7 @@ void run_green(Spectral &sp, int mode, const CGState *st, cudaStream_t s) {
   {                                                              \
     auto k = k_green<R, MODE, DD>;                               \
     allow_smem(k);                                               \
-    k<<<c.blocks, kPassThreads, c.smem, s>>>(a);                 \
+    k<<<c.blocks, c.threads, c.smem, s>>>(a);                 \
   }
   if (mode == GM_FWD) MUSG_GREEN(GM_FWD, 2)
   else if (mode == GM_INV) MUSG_GREEN(GM_INV, 2)
@@ -313,6 +319,73 @@ void tangent_operator(Spectral &sp, int tkind, const TangentData<R> &td, const R
   launch_inv<R, EPI_PLAIN, 0>(a, c, s);
 }
 
+// Autotuner: candidate (threads, shared-memory target) per pass, each timed with
+// CUDA events over `reps` launches on a scratch field; the fastest is kept.
+template <typename R> void spectral_autotune(Spectral &sp, cudaStream_t s, int effort) {
+  const int pi = prec_index<R>();
+  const long long n = (long long)sp.g.npx * sp.ncomp;
+  R *field = nullptr;
+  MUSG_CUDA(cudaMalloc(&field, (size_t)n * sizeof(R)));
+  MUSG_CUDA(cudaMemsetAsync(field, 0, (size_t)n * sizeof(R), s));
+  cudaEvent_t e0, e1;
+  MUSG_CUDA(cudaEventCreate(&e0));
+  MUSG_CUDA(cudaEventCreate(&e1));
+  const int reps = effort >= 2 ? 5 : 3;
+  const int threads[] = {128, 256, 512};
+  const long bytes[] = {16384, 32768, 49152, 73728, 110592, 225280};
+  const int gm = sp.proj_kind >= 0 ? green_mode_of(sp) : GM_FWD;
+  try {
+    for (int pass = 0; pass < 3; ++pass) {
+      if (pass == 1 && sp.g.dim != 3) continue;
+      float best = 1e30f;
+      int bt = sp.tune_threads[pi][pass];
+      long bb = sp.tune_bytes[pi][pass];
+      for (int th : threads)
+        for (long by : bytes) {
+          sp.tune_threads[pi][pass] = th;
+          sp.tune_bytes[pi][pass] = by;
+          float tot = 0;
+          for (int r = -1; r < reps; ++r) {
+            MUSG_CUDA(cudaEventRecord(e0, s));
+            if (pass == 0) {
+              const Cfg c = last_cfg<R>(sp);
+              LastArgs<R> a = last_args<R>(sp, c);
+              a.in = field;
+              a.out = field;
+              a.scale = R(1);
+              dispatch_fwd<R, PRO_PLAIN>(sp.g.dim, TK_PLAIN, a, c, s);
+              launch_inv<R, EPI_PLAIN, 0>(a, c, s);
+            } else if (pass == 1) {
+              run_axis<R>(sp, false, nullptr, s);
+            } else {
+              run_green<R>(sp, gm, nullptr, s);
+            }
+            MUSG_CUDA(cudaEventRecord(e1, s));
+            MUSG_CUDA(cudaEventSynchronize(e1));
+            float ms = 0;
+            MUSG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+            if (r >= 0) tot += ms;
+          }
+          if (tot < best) {
+            best = tot;
+            bt = th;
+            bb = by;
+          }
+        }
+      sp.tune_threads[pi][pass] = bt;
+      sp.tune_bytes[pi][pass] = bb;
+    }
+  } catch (...) {
+    cudaFree(field);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    throw;
+  }
+  cudaFree(field);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+}
+
 #define MUSG_INSTANTIATE_SPECTRAL(R)                                                               \
   template void spectral_forward<R>(Spectral &, const R *, R, cudaStream_t);                      \
   template void spectral_inverse<R>(Spectral &, R *, R, cudaStream_t);                            \
@@ -320,6 +393,7 @@ void tangent_operator(Spectral &sp, int tkind, const TangentData<R> &td, const R
   template int cg_operator<R>(Spectral &, int, const TangentData<R> &, const CGState *, const R *, \
                               R *, R *, double *, cudaStream_t, cudaEvent_t *);                    \
   template void tangent_operator<R>(Spectral &, int, const TangentData<R> &, const R *, R *,       \
-                                    cudaStream_t);
+                                    cudaStream_t);                                                 \
+  template void spectral_autotune<R>(Spectral &, cudaStream_t, int);
 
 }  // namespace musg

@@ -92,11 +92,13 @@ def voronoi(n=64, nseeds=32, nsteps=20, seed=11):
                 steps=steps, cg_tol=1e-8, maxiter=4000, newton_tol=1e-6, equil_tol=0.0, seed=seed)
 
 
-def build_spheres_cell(mu, w, allow_even=True):
+def build_spheres_cell(mu, w, allow_even=True, flags=None):
+    """The GPU cell; ``flags`` = FFT_PlanFlags (default: measure, i.e. autotuned launch
+    shapes, as the reference's demonstrators plan with FFTW_MEASURE)."""
     cell = mu.Cell(w['res'], w['lengths'], mu.Formulation.finite_strain, allow_even=allow_even)
     mu.material.MaterialLinearElastic1_3d.make(cell, 'inclusions', w['E_incl'], w['nu']).add_pixels(w['inside'])
     mu.material.MaterialLinearElastic1_3d.make(cell, 'matrix', w['E_matrix'], w['nu']).add_pixels(~w['inside'])
-    cell.initialise()
+    cell.initialise(mu.FFT_PlanFlags.measure if flags is None else flags)
     return cell
 
 

@@ -456,3 +456,19 @@ def test_hep1_load_steps(mu):
     for a, b in zip(rg, ro):
         assert (a.nb_it, a.nb_fev) == (b.nb_it, b.nb_fev)
         assert rel(a.stress, b.stress) < 1e-8
+
+
+def test_autotuned_shapes_same_results(mu):
+    """FFT_PlanFlags.measure (autotuned launch shapes) changes only the speed: the
+    mixed and FP64 solves agree with the default shapes."""
+    from muspectre_gb300 import workloads
+    w = workloads.spheres(32, nsph=6)
+    out = []
+    for flags in (mu.FFT_PlanFlags.estimate, mu.FFT_PlanFlags.measure):
+        cell = workloads.build_spheres_cell(mu, w, flags=flags)
+        r = mu.solvers.newton_cg(cell, w['load'], mu.solvers.SolverCG(cell, 1e-8, 2000), 1e-6, 0.0)
+        out.append((r, cell.tuning()))
+    (a, ta), (b, tb) = out
+    assert (a.nb_it, a.nb_fev) == (b.nb_it, b.nb_fev)
+    assert rel(a.grad, b.grad) < 1e-12
+    assert all(t[0] in (128, 256, 512) for t in tb['fp64'].values())
