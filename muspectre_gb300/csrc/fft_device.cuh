@@ -1,6 +1,7 @@
 // Shared-memory FFT core for pencils of one axis (device code).
 //
-// Algorithm: Stockham auto-sort FFT (decimation in time), mixed radix 2/3/4/5/7/8,
+// Algorithm: Stockham auto-sort FFT (decimation in time), mixed radix
+// 2/3/4/5/7/8/9/16 (9 and 16 as 3x3 and 4x4 in registers),
 // in the formulation of Govindaraju et al., "High performance discrete Fourier
 // transforms on graphics processors" (SC'08): for each stage of radix R with span
 // Ns (product of the radices already applied),
@@ -185,6 +186,70 @@ template <int P, bool INV, typename T> struct DftPrime {
   }
 };
 
+// cos/sin(2 pi j / N) for the composite radices 16 and 9 (j < N)
+template <int N> struct CompCS;
+template <> struct CompCS<16> {
+  static __device__ __forceinline__ double c(int j) {
+    constexpr double a = 0.9238795325112867561282, b = 0.7071067811865475244008, g = 0.3826834323650897717285;
+    return j == 0 ? 1.0 : j == 1 ? a : j == 2 ? b : j == 3 ? g : j == 4 ? 0.0 : j == 5 ? -g : j == 6 ? -b
+           : j == 7 ? -a : j == 8 ? -1.0 : j == 9 ? -a : j == 10 ? -b : j == 11 ? -g : j == 12 ? 0.0
+           : j == 13 ? g : j == 14 ? b : a;
+  }
+  static __device__ __forceinline__ double s(int j) { return c((j + 12) & 15); }  // sin x = cos(x - pi/2)
+};
+template <> struct CompCS<9> {
+  static __device__ __forceinline__ double c(int j) {
+    return j == 0 ? 1.0 : (j == 1 || j == 8) ? 0.7660444431189780352024 : (j == 2 || j == 7) ? 0.1736481776669303488517
+           : (j == 3 || j == 6) ? -0.5 : -0.9396926207859083840541;
+  }
+  static __device__ __forceinline__ double s(int j) {
+    return j == 0 ? 0.0 : j == 1 ? 0.6427876096865393263226 : j == 2 ? 0.9848077530122080593667
+           : j == 3 ? 0.8660254037844386467637 : j == 4 ? 0.3420201433256687330441
+           : j == 5 ? -0.3420201433256687330441 : j == 6 ? -0.8660254037844386467637
+           : j == 7 ? -0.9848077530122080593667 : -0.6427876096865393263226;
+  }
+};
+
+// composite radix N = N1 * N2 in registers (Cooley-Tukey): N2 DFTs of length N1 over
+// the stride-N2 subsequences, twiddles W_N^(n2 k1), then N1 DFTs of length N2
+template <int N1, int N2, bool INV, typename T> struct DftComposite {
+  static __device__ __forceinline__ void run(T *v) {
+    using R = decltype(v[0].x);
+    constexpr int N = N1 * N2;
+    T a[N2][N1];
+#pragma unroll
+    for (int n2 = 0; n2 < N2; ++n2) {
+#pragma unroll
+      for (int n1 = 0; n1 < N1; ++n1) a[n2][n1] = v[N2 * n1 + n2];
+      Dft<N1, INV, T>::run(a[n2]);
+#pragma unroll
+      for (int k1 = 1; k1 < N1; ++k1) {
+        const int j = (n2 * k1) % N;
+        if (j == 0) continue;
+        const R c = R(CompCS<N>::c(j)), sn = R(CompCS<N>::s(j));
+        const T w = INV ? T{c, sn} : T{c, -sn};
+        a[n2][k1] = cmul(a[n2][k1], w);
+      }
+    }
+#pragma unroll
+    for (int k1 = 0; k1 < N1; ++k1) {
+      T b[N2];
+#pragma unroll
+      for (int n2 = 0; n2 < N2; ++n2) b[n2] = a[n2][k1];
+      Dft<N2, INV, T>::run(b);
+#pragma unroll
+      for (int k2 = 0; k2 < N2; ++k2) v[k1 + N1 * k2] = b[k2];
+    }
+  }
+};
+
+template <bool INV, typename T> struct Dft<16, INV, T> {
+  static __device__ __forceinline__ void run(T *v) { DftComposite<4, 4, INV, T>::run(v); }
+};
+template <bool INV, typename T> struct Dft<9, INV, T> {
+  static __device__ __forceinline__ void run(T *v) { DftComposite<3, 3, INV, T>::run(v); }
+};
+
 template <bool INV, typename T> struct Dft<5, INV, T> {
   static __device__ __forceinline__ void run(T *v) { DftPrime<5, INV, T>::run(v); }
 };
@@ -235,15 +300,17 @@ __device__ __forceinline__ typename V2<R>::T *fft_stages(typename V2<R>::T *a, t
   int Ns = 1;
   unsigned long long code = ap.rcode;
   T *src = a, *dst = b;
-  for (int s = 0; s < ap.nst; ++s, code >>= 4) {
-    const int rad = (int)(code & 15ull);
+  for (int s = 0; s < ap.nst; ++s, code >>= 5) {
+    const int rad = (int)(code & 31ull);
     switch (rad) {
       case 2: fft_stage<R, 2, INV>(src, dst, P, ap.m, Ns, ap.tw); break;
       case 3: fft_stage<R, 3, INV>(src, dst, P, ap.m, Ns, ap.tw); break;
       case 4: fft_stage<R, 4, INV>(src, dst, P, ap.m, Ns, ap.tw); break;
       case 5: fft_stage<R, 5, INV>(src, dst, P, ap.m, Ns, ap.tw); break;
       case 7: fft_stage<R, 7, INV>(src, dst, P, ap.m, Ns, ap.tw); break;
-      default: fft_stage<R, 8, INV>(src, dst, P, ap.m, Ns, ap.tw); break;
+      case 9: fft_stage<R, 9, INV>(src, dst, P, ap.m, Ns, ap.tw); break;
+      case 8: fft_stage<R, 8, INV>(src, dst, P, ap.m, Ns, ap.tw); break;
+      default: fft_stage<R, 16, INV>(src, dst, P, ap.m, Ns, ap.tw); break;
     }
     Ns *= rad;
     T *t = src;

@@ -41,7 +41,7 @@ template <typename R> struct V2;
 template <> struct V2<float> { using T = float2; };
 template <> struct V2<double> { using T = double2; };
 
-constexpr int kMaxStages = 16;
+constexpr int kMaxStages = 12;  // 5 bits per stage in AxisPlanD::rcode
 constexpr int kMaxMaterials = 256;
 
 // ---------------------------------------------------------------- FFT plans
@@ -53,7 +53,7 @@ template <typename R> struct AxisPlanD {
   int m;
   int nst;
   int blu;
-  unsigned long long rcode;  // radix of stage s in bits [4s, 4s+4)
+  unsigned long long rcode;  // radix of stage s in bits [5s, 5s+5)
   const typename V2<R>::T *tw;    // m entries: exp(-2 pi i j / m)
   const typename V2<R>::T *chirp; // n entries: exp(-pi i j^2 / n)     (Bluestein)
   const typename V2<R>::T *bf;    // m entries: DFT_m(conj chirp)/m     (Bluestein)

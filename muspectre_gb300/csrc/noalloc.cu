@@ -64,11 +64,14 @@ bool factor_fixed(int n, int *rad, int &nst) {
     ++nst;
   };
   while (k > 0) {
-    if (k == 4) { push(4); push(4); k = 0; }
-    else if (k >= 3) { push(8); k -= 3; }
+    if (k >= 4 && k != 5 && k != 6) { push(16); k -= 4; }
+    else if (k == 6) { push(8); push(8); k = 0; }
+    else if (k == 5) { push(8); push(4); k = 0; }
+    else if (k == 3) { push(8); k = 0; }
     else if (k == 2) { push(4); k = 0; }
     else { push(2); k = 0; }
   }
+  while (n % 9 == 0) { push(9); n /= 9; }
   for (int r : {3, 5, 7})
     while (n % r == 0) { push(r); n /= r; }
   return n == 1 && nst <= kMaxStages;

@@ -35,12 +35,16 @@ bool factorize(int n, std::vector<int> &out) {
   out.clear();
   int k = 0;
   while (n % 2 == 0) { n /= 2; ++k; }
+  // powers of two: radix 16 as long as possible, the remainder as balanced 8/4
   while (k > 0) {
-    if (k == 4) { out.push_back(4); out.push_back(4); k = 0; }
-    else if (k >= 3) { out.push_back(8); k -= 3; }
+    if (k >= 4 && k != 5 && k != 6) { out.push_back(16); k -= 4; }
+    else if (k == 6) { out.push_back(8); out.push_back(8); k = 0; }
+    else if (k == 5) { out.push_back(8); out.push_back(4); k = 0; }
+    else if (k == 3) { out.push_back(8); k = 0; }
     else if (k == 2) { out.push_back(4); k = 0; }
     else { out.push_back(2); k = 0; }
   }
+  while (n % 9 == 0) { out.push_back(9); n /= 9; }
   for (int r : {3, 5, 7})
     while (n % r == 0) { out.push_back(r); n /= r; }
   return n == 1;
@@ -152,7 +156,7 @@ template <> AxisPlanD<double> AxisPlan::device<double>() const {
   AxisPlanD<double> d{};
   d.n = n; d.m = m; d.nst = nst; d.blu = blu;
   d.rcode = 0;
-  for (int s = 0; s < nst; ++s) d.rcode |= (unsigned long long)radix[s] << (4 * s);
+  for (int s = 0; s < nst; ++s) d.rcode |= (unsigned long long)radix[s] << (5 * s);
   d.tw = (const double2 *)tw64;
   d.chirp = (const double2 *)chirp64;
   d.bf = (const double2 *)bf64;
@@ -163,7 +167,7 @@ template <> AxisPlanD<float> AxisPlan::device<float>() const {
   AxisPlanD<float> d{};
   d.n = n; d.m = m; d.nst = nst; d.blu = blu;
   d.rcode = 0;
-  for (int s = 0; s < nst; ++s) d.rcode |= (unsigned long long)radix[s] << (4 * s);
+  for (int s = 0; s < nst; ++s) d.rcode |= (unsigned long long)radix[s] << (5 * s);
   d.tw = (const float2 *)tw32;
   d.chirp = (const float2 *)chirp32;
   d.bf = (const float2 *)bf32;

@@ -32,7 +32,7 @@ def rel(a, b):
 
 
 # ------------------------------------------------------------------ FFT engine
-@pytest.mark.parametrize('res', [[6, 4], [5, 7], [51, 51], [17, 13], [8, 6, 4], [5, 7, 9], [15, 11, 13],
+@pytest.mark.parametrize('res', [[6, 4], [5, 7], [51, 51], [17, 13], [8, 6, 4], [5, 7, 9], [15, 11, 13], [128, 48], [256, 81],
                                  [16, 16, 16], [34, 21], [64, 64, 64]])
 def test_fft_vs_numpy(mu, res):
     """python_fft_tests.py:60-101 (tolerance 1e-14·N), over radix-2/3/5/7 and
