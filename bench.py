@@ -42,8 +42,8 @@ sys.path.insert(0, ROOT)
 # Newton and CG iteration counts of the FP64 method on this exact seeded input
 # (identical between the oracle and the GPU FP64 path, as the parity tests check);
 # the CPU runs time a bounded sample and scale by them
-REF_NEWTON_STEPS = None
-REF_CG_ITERS = None
+REF_NEWTON_STEPS = 4
+REF_CG_ITERS = 530
 
 
 def parse():

@@ -66,6 +66,7 @@ typedef struct musg_cell musg_cell;
 typedef struct musg_solver musg_solver;
 typedef struct musg_fft musg_fft;
 typedef struct musg_projection musg_projection;
+typedef struct musg_batch musg_batch;
 
 /* OptimizeResult (src/solver/solver_common.hh:50-67) without its two field arrays,
  * which musg_newton_cg writes into caller buffers. */
@@ -159,6 +160,23 @@ int musg_newton_cg(musg_cell *cell, const double *load_steps, int nb_steps,
                    musg_solver *solver, double newton_tol, double equil_tol,
                    int verbose, musg_result_info *infos, double *grads,
                    double *stresses);
+
+/* -------------------------------------------------------------- batches
+ * Many same-shape cells (RVEs, or right-hand sides on copies of one microstructure)
+ * solved together: newton_cg's Newton steps run in lockstep per cell and every CG
+ * iteration is one launch per pass for all cells (replayed from one CUDA graph).
+ * No counterpart in the reference, which solves one cell at a time; each cell's
+ * results equal those of musg_newton_cg on it alone.  load_steps: nb_cells x
+ * nb_steps D*D column-major matrices; infos: nb_cells x nb_steps records; stresses
+ * (may be NULL): nb_cells x nb_steps x nb_dof.  A cell whose CG fails is reported
+ * (success 0, the ConvergenceError message) and leaves the batch. */
+int musg_batch_create(musg_cell **cells, int nb_cells, double tol, unsigned maxiter,
+                      int precision, musg_batch **out);
+int musg_batch_destroy(musg_batch *batch);
+int musg_batch_set_inner_tol(musg_batch *batch, double inner_tol);
+int musg_batch_newton_cg(musg_batch *batch, const double *load_steps, int nb_steps,
+                         double newton_tol, double equil_tol, musg_result_info *infos,
+                         double *stresses);
 
 /* ---------------------------------------------------------- instrumentation
  * (no counterpart in the reference, which has no device)

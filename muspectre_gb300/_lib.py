@@ -80,6 +80,10 @@ _SIGNATURES = {
     'musg_solver_solve': (C.c_int, [_P, _D, _D]),
     'musg_newton_cg': (C.c_int, [_P, _D, C.c_int, _P, C.c_double, C.c_double, C.c_int, C.POINTER(ResultInfo), _D,
                                  _D]),
+    'musg_batch_create': (C.c_int, [C.POINTER(_P), C.c_int, C.c_double, C.c_uint, C.c_int, C.POINTER(_P)]),
+    'musg_batch_destroy': (C.c_int, [_P]),
+    'musg_batch_set_inner_tol': (C.c_int, [_P, C.c_double]),
+    'musg_batch_newton_cg': (C.c_int, [_P, _D, C.c_int, C.c_double, C.c_double, C.POINTER(ResultInfo), _D]),
     'musg_launch_count': (C.c_int, [C.POINTER(C.c_ulonglong)]),
     'musg_solver_profile': (C.c_int, [_P, C.c_int, _D, _I]),
     'musg_solver_kernel_name': (C.c_char_p, [_P, C.c_int]),

@@ -609,6 +609,124 @@ struct musg_solver {
   }
 };
 
+// ---------------------------------------------------------------------- batches
+// Same-shape cells solved together: Newton steps in lockstep, every CG iteration one
+// launch per pass for all cells (problem b = blockIdx.y), captured in one graph.
+struct musg_batch {
+  std::vector<musg_cell *> cells;
+  std::vector<std::unique_ptr<musg_solver>> solvers;  // per-cell vectors
+  int precision = MUSG_PRECISION_FP64;
+  double tol = 0, inner_tol = 1e-5;
+  unsigned maxiter = 0;
+  cudaStream_t stream = nullptr;
+  DevBuf states, tab_p, tab_v;
+  CGState *hst = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  unsigned long long graph_nodes = 0;
+  int chunk = 16;
+
+  ~musg_batch() {
+    if (exec) cudaGraphExecDestroy(exec);
+    if (hst) cudaFreeHost(hst);
+    if (stream) cudaStreamDestroy(stream);
+  }
+  int B() const { return (int)cells.size(); }
+  CGState *state(int b) const { return states.as<CGState>() + b; }
+
+  template <typename R> void build_tables() {
+    std::vector<ProblemPtrsHost> tp(B());
+    std::vector<BatchVec<R>> tv(B());
+    for (int b = 0; b < B(); ++b) {
+      musg_cell &c = *cells[b];
+      musg_solver &sv = *solvers[b];
+      const TangentData<R> td = c.tangent<R>();
+      tp[b].spec = sizeof(R) == 8 ? c.sp.spec64 : c.sp.spec32;
+      tp[b].st = state(b);
+      tp[b].r = sv.r.p;
+      tp[b].p = sv.p.p;
+      tp[b].Ap = sv.Ap.p;
+      tp[b].partial = c.partial.as<double>();
+      static_assert(sizeof(TangentData<R>) == sizeof(tp[b].td), "tangent table layout");
+      memcpy(tp[b].td, &td, sizeof(td));
+      tv[b].st = state(b);
+      tv[b].x = sv.x.as<R>();
+      tv[b].r = sv.r.as<R>();
+      tv[b].p = sv.p.as<R>();
+      tv[b].Ap = sv.Ap.as<R>();
+      tv[b].partial = c.partial.as<double>();
+    }
+    tab_p.alloc(tp.size() * sizeof(ProblemPtrsHost));
+    tab_v.alloc(tv.size() * sizeof(BatchVec<R>));
+    MUSG_CUDA(cudaMemcpy(tab_p.p, tp.data(), tab_p.bytes, cudaMemcpyHostToDevice));
+    MUSG_CUDA(cudaMemcpy(tab_v.p, tv.data(), tab_v.bytes, cudaMemcpyHostToDevice));
+  }
+
+  template <typename R> void iteration(cudaStream_t s) {
+    musg_cell &c0 = *cells[0];
+    const long long n = c0.nb_dof();
+    const int nop = cg_operator_batch<R>(c0.sp, c0.tkind, (const ProblemPtrs<R> *)tab_p.p, B(), s);
+    cg_finalize_alpha_batch<R>(tab_v.as<BatchVec<R>>(), nop, B(), s);
+    cg_update_batch<R>(tab_v.as<BatchVec<R>>(), n, B(), s);
+    cg_finalize_beta_batch<R>(tab_v.as<BatchVec<R>>(), reduce_blocks(n), B(), s);
+  }
+
+  template <typename R> void build_graph() {
+    if (exec) return;
+    cudaGraph_t g = nullptr;
+    const unsigned long long before = g_launches.load();
+    MUSG_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeRelaxed));
+    try {
+      for (int k = 0; k < chunk; ++k) iteration<R>(stream);
+    } catch (...) {
+      cudaStreamEndCapture(stream, &g);
+      if (g) cudaGraphDestroy(g);
+      throw;
+    }
+    MUSG_CUDA(cudaStreamEndCapture(stream, &g));
+    graph_nodes = g_launches.load() - before;
+    g_launches.fetch_sub(graph_nodes);
+    MUSG_CUDA(cudaGraphInstantiate(&exec, g, 0));
+    cudaGraphDestroy(g);
+  }
+
+  // one batched SolverCG::solve over the cells whose `solve` flag is set
+  template <typename R> void solve(const std::vector<char> &solve_it, std::vector<std::string> &errors) {
+    const long long n = cells[0]->nb_dof();
+    const double t = (precision == MUSG_PRECISION_MIXED) ? std::max(tol, inner_tol) : tol;
+    for (int b = 0; b < B(); ++b) {
+      musg_cell &c = *cells[b];
+      double *part = c.partial.as<double>();
+      if (solve_it[b]) {
+        cg_init<R>(state(b), c.rhs.as<double>(), solvers[b]->r.as<R>(), solvers[b]->x.as<R>(), n, t, (int)maxiter,
+                   part, part + 4096, stream);
+      } else {
+        MUSG_CUDA(cudaMemsetAsync(&state(b)->active, 0, sizeof(int), stream));
+      }
+    }
+    build_graph<R>();
+    for (;;) {
+      MUSG_CUDA(cudaGraphLaunch(exec, stream));
+      g_launches.fetch_add(graph_nodes);
+      MUSG_CUDA(cudaMemcpyAsync(hst, states.p, B() * sizeof(CGState), cudaMemcpyDeviceToHost, stream));
+      MUSG_CUDA(cudaStreamSynchronize(stream));
+      bool any = false;
+      for (int b = 0; b < B(); ++b) any = any || hst[b].active;
+      if (!any) break;
+    }
+    for (int b = 0; b < B(); ++b) {
+      solvers[b]->counter = hst[b].counter;
+      if (!solve_it[b]) continue;
+      if (!(hst[b].rdr < hst[b].tol2)) {
+        std::ostringstream e;
+        e << "Conjugate gradient has not converged. After " << hst[b].counter
+          << " steps, the solver  FAILED with  |r|/|b| = " << std::sqrt(hst[b].rdr / hst[b].rhs_norm2)
+          << ", cg_tol = " << std::sqrt(hst[b].tol2 / hst[b].rhs_norm2);
+        errors[b] = e.str();
+      }
+    }
+  }
+};
+
 // ---------------------------------------------------------------------- FFT / projection handles
 struct musg_fft {
   Spectral sp;
@@ -730,6 +848,138 @@ void newton_cg_impl(musg_cell *cell, const double *steps, int nsteps, musg_solve
     if (grads) c.download_field(c.F.as<double>(), grads + (size_t)step * n);
     if (stresses) c.download_field(c.P.as<double>(), stresses + (size_t)step * n);
     c.save_history();
+  }
+  MUSG_CUDA(cudaStreamSynchronize(s));
+}
+
+// newton_cg (solvers.cc:44-217) for a batch of cells in lockstep; a cell that fails
+// (ConvergenceError) is reported in its result records and leaves the batch
+void batch_newton_impl(musg_batch *batch, const double *steps, int nsteps, double newton_tol, double equil_tol,
+                       musg_result_info *infos, double *stresses) {
+  require(batch && steps && nsteps > 0, MUSG_ERR_ARGUMENT, "invalid batch newton_cg arguments");
+  musg_batch &bt = *batch;
+  const int B = bt.B();
+  musg_cell &c0 = *bt.cells[0];
+  const int dim = c0.dim, D2 = c0.D2;
+  const long long n = c0.nb_dof();
+  cudaStream_t s = bt.stream;
+  std::vector<cudaStream_t> saved(B);
+  for (int b = 0; b < B; ++b) {
+    saved[b] = bt.cells[b]->stream;
+    bt.cells[b]->stream = s;
+  }
+  struct Restore {
+    musg_batch &bt;
+    std::vector<cudaStream_t> &saved;
+    ~Restore() {
+      for (int b = 0; b < bt.B(); ++b) bt.cells[b]->stream = saved[b];
+    }
+  } restore{bt, saved};
+  std::vector<double> I(D2, 0.0);
+  if (c0.form == MUSG_FINITE_STRAIN)
+    for (int i = 0; i < dim; ++i) I[i + dim * i] = 1.0;
+  else
+    for (int k = 0; k < B * nsteps; ++k) check_symmetry_or_throw(steps + (size_t)k * D2, dim);
+  for (int b = 0; b < B; ++b)
+    fill_uniform(bt.cells[b]->F.as<double>(), bt.cells[b]->put_matrix(I.data(), 0), D2, c0.npx, s);
+  std::vector<std::vector<double>> previous(B, std::vector<double>(D2, 0.0));
+  std::vector<char> failed(B, 0);
+  std::vector<std::string> errmsg(B);
+  for (int step = 0; step < nsteps; ++step) {
+    std::vector<double> incr(B, 2 * newton_tol), grad(B, 1.0), stress(B, 2 * equil_tol);
+    std::vector<char> conv(B, 0), running(B, 0);
+    std::vector<unsigned> newt(B, 0);
+    std::vector<std::string> message(B, "Has not converged");
+    auto test = [&](int b) {
+      const bool incr_test = incr[b] / grad[b] <= newton_tol;
+      const bool stress_test = stress[b] < equil_tol;
+      if (incr_test) message[b] = "Residual  tolerance reached";
+      else if (stress_test) message[b] = "Reached stress divergence tolerance";
+      conv[b] = incr_test || stress_test;
+      return (bool)conv[b];
+    };
+    for (int b = 0; b < B; ++b) {
+      if (failed[b]) continue;
+      musg_cell &c = *bt.cells[b];
+      const double *macro = steps + ((size_t)b * nsteps + step) * D2;
+      std::vector<double> delta(D2);
+      for (int k = 0; k < D2; ++k) delta[k] = macro[k] - previous[b][k];
+      add_macro(c.F.as<double>(), c.put_matrix(delta.data(), 16), D2, c.npx, s);
+      previous[b].assign(macro, macro + D2);
+      running[b] = 1;
+    }
+    for (;;) {
+      // Newton iteration: evaluate, residual, convergence (per cell)
+      std::vector<char> solve_it(B, 0);
+      bool any = false;
+      for (int b = 0; b < B; ++b) {
+        if (!running[b] || newt[b] >= bt.maxiter) {
+          running[b] = 0;
+          continue;
+        }
+        musg_cell &c = *bt.cells[b];
+        c.evaluate(false);
+        spectral_project<double>(c.sp, c.P.as<double>(), c.rhs.as<double>(), -1.0, s);
+        dot_device<double, double>(c.rhs.as<double>(), c.rhs.as<double>(), n, c.partial.as<double>(),
+                                   c.scal.as<double>() + 32, s);
+        MUSG_CUDA(cudaMemcpyAsync(c.hscal + 32, c.scal.as<double>() + 32, sizeof(double), cudaMemcpyDeviceToHost, s));
+      }
+      MUSG_CUDA(cudaStreamSynchronize(s));
+      for (int b = 0; b < B; ++b) {
+        if (!running[b]) continue;
+        stress[b] = std::sqrt(bt.cells[b]->hscal[32]);
+        if (test(b)) {
+          running[b] = 0;
+          continue;
+        }
+        solve_it[b] = 1;
+        any = true;
+      }
+      if (!any) break;
+      std::vector<std::string> errors(B);
+      if (bt.precision == MUSG_PRECISION_MIXED) bt.solve<float>(solve_it, errors);
+      else bt.solve<double>(solve_it, errors);
+      for (int b = 0; b < B; ++b) {
+        if (!solve_it[b]) continue;
+        if (!errors[b].empty()) {
+          failed[b] = 1;
+          running[b] = 0;
+          errmsg[b] = errors[b];
+          continue;
+        }
+        musg_cell &c = *bt.cells[b];
+        double *dscal = c.scal.as<double>();
+        if (bt.precision == MUSG_PRECISION_MIXED)
+          newton_update<float>(c.F.as<double>(), bt.solvers[b]->x.as<float>(), n, c.partial.as<double>(), dscal + 34, s);
+        else
+          newton_update<double>(c.F.as<double>(), bt.solvers[b]->x.as<double>(), n, c.partial.as<double>(), dscal + 34,
+                                s);
+        MUSG_CUDA(cudaMemcpyAsync(c.hscal + 34, dscal + 34, 2 * sizeof(double), cudaMemcpyDeviceToHost, s));
+      }
+      MUSG_CUDA(cudaStreamSynchronize(s));
+      for (int b = 0; b < B; ++b) {
+        if (!solve_it[b] || failed[b]) continue;
+        incr[b] = std::sqrt(bt.cells[b]->hscal[34]);
+        grad[b] = std::sqrt(bt.cells[b]->hscal[35]);
+        test(b);
+        newt[b] += 1;
+        if (conv[b]) running[b] = 0;
+      }
+    }
+    for (int b = 0; b < B; ++b) {
+      musg_cell &c = *bt.cells[b];
+      if (!failed[b] && bt.precision == MUSG_PRECISION_MIXED && !c.has_hep) c.evaluate(false);
+      musg_result_info &ri = infos[(size_t)b * nsteps + step];
+      const bool ok = !failed[b] && test(b);
+      ri.success = ok ? 1 : 0;
+      ri.status = ok ? 1 : 0;
+      ri.nb_it = newt[b];
+      ri.nb_fev = (unsigned)bt.solvers[b]->counter;
+      memset(ri.message, 0, sizeof(ri.message));
+      strncpy(ri.message, failed[b] ? errmsg[b].c_str() : message[b].c_str(), sizeof(ri.message) - 1);
+      if (stresses && !failed[b]) c.download_field(c.P.as<double>(), stresses + ((size_t)b * nsteps + step) * n);
+      if (!failed[b]) c.save_history();
+    }
   }
   MUSG_CUDA(cudaStreamSynchronize(s));
 }
@@ -1026,6 +1276,64 @@ int musg_solver_profile(musg_solver *solver, int iterations, double *ms_out, int
 const char *musg_solver_kernel_name(musg_solver *solver, int k) {
   if (!solver || !solver->cell) return "";
   return musg_solver::kernel_name(solver->cell->dim, k);
+}
+
+int musg_batch_create(musg_cell **cells, int nb_cells, double tol, unsigned maxiter, int precision,
+                      musg_batch **out) {
+  return guard([&] {
+    require(out && cells && nb_cells > 0, MUSG_ERR_ARGUMENT, "invalid argument");
+    auto bt = std::make_unique<musg_batch>();
+    musg_cell &c0 = *cells[0];
+    for (int b = 0; b < nb_cells; ++b) {
+      musg_cell &c = *cells[b];
+      require(cells[b] != nullptr, MUSG_ERR_ARGUMENT, "null cell");
+      if (!c.initialised) c.initialise();
+      require(c.dim == c0.dim && c.form == c0.form && c.res[0] == c0.res[0] && c.res[1] == c0.res[1] &&
+                  c.res[2] == c0.res[2] && c.flags == c0.flags && c.tkind == c0.tkind,
+              MUSG_ERR_ARGUMENT, "cells of a batch need the same grid, formulation and material-law kind");
+      for (int k = 0; k < b; ++k) require(cells[k] != cells[b], MUSG_ERR_ARGUMENT, "a cell appears twice in a batch");
+      auto sv = std::make_unique<musg_solver>();
+      sv->create(&c, tol, maxiter, 0, precision);
+      bt->solvers.push_back(std::move(sv));
+      bt->cells.push_back(&c);
+    }
+    // the launch shapes of the first cell serve the whole batch
+    for (int b = 1; b < nb_cells; ++b)
+      for (int p = 0; p < 2; ++p)
+        for (int k = 0; k < 3; ++k) {
+          cells[b]->sp.tune_threads[p][k] = c0.sp.tune_threads[p][k];
+          cells[b]->sp.tune_bytes[p][k] = c0.sp.tune_bytes[p][k];
+        }
+    bt->precision = precision;
+    bt->tol = tol;
+    bt->maxiter = maxiter;
+    MUSG_CUDA(cudaStreamCreateWithFlags(&bt->stream, cudaStreamNonBlocking));
+    bt->states.alloc(nb_cells * sizeof(CGState));
+    MUSG_CUDA(cudaMemset(bt->states.p, 0, bt->states.bytes));
+    MUSG_CUDA(cudaMallocHost(&bt->hst, nb_cells * sizeof(CGState)));
+    if (precision == MUSG_PRECISION_MIXED) bt->build_tables<float>();
+    else bt->build_tables<double>();
+    *out = bt.release();
+  });
+}
+
+int musg_batch_destroy(musg_batch *batch) {
+  return guard([&] { delete batch; });
+}
+
+int musg_batch_set_inner_tol(musg_batch *batch, double inner_tol) {
+  return guard([&] {
+    require(batch && inner_tol >= 0, MUSG_ERR_ARGUMENT, "invalid argument");
+    batch->inner_tol = inner_tol;
+  });
+}
+
+int musg_batch_newton_cg(musg_batch *batch, const double *load_steps, int nb_steps, double newton_tol,
+                         double equil_tol, musg_result_info *infos, double *stresses) {
+  return guard([&] {
+    require(infos, MUSG_ERR_ARGUMENT, "null result records");
+    batch_newton_impl(batch, load_steps, nb_steps, newton_tol, equil_tol, infos, stresses);
+  });
 }
 
 int musg_newton_cg(musg_cell *cell, const double *load_steps, int nb_steps, musg_solver *solver, double newton_tol,

@@ -132,6 +132,68 @@ void cg_finalize_beta(CGState *st, const double *partial, int nparts, cudaStream
   MUSG_CHECK_LAUNCH();
 }
 
+// ------------------------------------------------------------------ batched
+template <typename R>
+__global__ void k_cg_update_b(const BatchVec<R> *tab, long long n) {
+  const BatchVec<R> q = tab[blockIdx.y];
+  if (!q.st->active) return;
+  const R alpha = R(q.st->alpha);
+  Acc<R> acc;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    q.x[i] += alpha * q.p[i];
+    const R rv = q.r[i] + alpha * q.Ap[i];
+    q.r[i] = rv;
+    acc.add(rv * rv);
+  }
+  const double bs = block_sum(acc.value());
+  if (threadIdx.x == 0) q.partial[blockIdx.x] = bs;
+}
+
+template <typename R> __global__ void k_cg_alpha_b(const BatchVec<R> *tab, int nparts) {
+  CGState *st = tab[blockIdx.x].st;
+  if (!st->active) return;
+  const double pAp = sum_partials(tab[blockIdx.x].partial, nparts);
+  if (threadIdx.x == 0) {
+    st->pAp = pAp;
+    st->alpha = st->rdr / pAp;
+  }
+}
+
+template <typename R> __global__ void k_cg_beta_b(const BatchVec<R> *tab, int nparts) {
+  CGState *st = tab[blockIdx.x].st;
+  if (!st->active) return;
+  const double new_rdr = sum_partials(tab[blockIdx.x].partial, nparts);
+  if (threadIdx.x == 0) {
+    st->beta = new_rdr / st->rdr;
+    st->rdr = new_rdr;
+    st->iter += 1;
+    st->counter += 1;
+    if (!(st->iter < st->maxiter && st->rdr > st->tol2)) st->active = 0;
+  }
+}
+
+template <typename R> void cg_update_batch(const BatchVec<R> *tab, long long n, int B, cudaStream_t s) {
+  k_cg_update_b<R><<<dim3(reduce_blocks(n), B), kRedThreads, 0, s>>>(tab, n);
+  MUSG_CHECK_LAUNCH();
+}
+
+template <typename R> void cg_finalize_alpha_batch(const BatchVec<R> *tab, int nparts, int B, cudaStream_t s) {
+  k_cg_alpha_b<R><<<B, 1024, 0, s>>>(tab, nparts);
+  MUSG_CHECK_LAUNCH();
+}
+
+template <typename R> void cg_finalize_beta_batch(const BatchVec<R> *tab, int nparts, int B, cudaStream_t s) {
+  k_cg_beta_b<R><<<B, 1024, 0, s>>>(tab, nparts);
+  MUSG_CHECK_LAUNCH();
+}
+
+template void cg_update_batch<double>(const BatchVec<double> *, long long, int, cudaStream_t);
+template void cg_update_batch<float>(const BatchVec<float> *, long long, int, cudaStream_t);
+template void cg_finalize_alpha_batch<double>(const BatchVec<double> *, int, int, cudaStream_t);
+template void cg_finalize_alpha_batch<float>(const BatchVec<float> *, int, int, cudaStream_t);
+template void cg_finalize_beta_batch<double>(const BatchVec<double> *, int, int, cudaStream_t);
+template void cg_finalize_beta_batch<float>(const BatchVec<float> *, int, int, cudaStream_t);
+
 // ------------------------------------------------------------------ dots
 template <typename Ra, typename Rb>
 __global__ void k_dot(const Ra *__restrict__ a, const Rb *__restrict__ b, long long n, double *partial) {

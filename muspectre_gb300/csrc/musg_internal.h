@@ -167,6 +167,21 @@ template <typename R>
 void tangent_operator(Spectral &sp, int tkind, const TangentData<R> &td, const R *in,
                       R *out, cudaStream_t s);
 int cg_operator_partials(const Spectral &sp);
+// batched CG operator over B same-shape problems (one launch per pass; problem b
+// is blockIdx.y); tab is a device array of B ProblemPtrs (spectral.cuh), whose host
+// image is ProblemPtrsHost
+template <typename R> struct ProblemPtrs;
+struct ProblemPtrsHost {
+  void *spec;
+  const CGState *st;
+  const void *r;
+  void *p;
+  void *Ap;
+  double *partial;
+  unsigned char td[sizeof(TangentData<double>)];
+};
+template <typename R>
+int cg_operator_batch(Spectral &sp, int tkind, const ProblemPtrs<R> *tab, int B, cudaStream_t s);
 // Times candidate launch shapes of each pass on this grid (CUDA events) and keeps
 // the fastest (FFT_PlanFlags::measure / patient); fp32 selects the FP32 passes.
 template <typename R> void spectral_autotune(Spectral &sp, cudaStream_t s, int effort);
@@ -181,6 +196,21 @@ void cg_update(const CGState *st, R *x, R *r, const R *p, const R *Ap, long long
                double *partial, cudaStream_t s);
 void cg_finalize_alpha(CGState *st, const double *partial, int nparts, cudaStream_t s);
 void cg_finalize_beta(CGState *st, const double *partial, int nparts, cudaStream_t s);
+// batched variants: per-problem pointer tables (device arrays of B entries)
+template <typename R> struct BatchVec {
+  CGState *st;
+  R *x;
+  R *r;
+  const R *p;
+  const R *Ap;
+  double *partial;
+};
+template <typename R>
+void cg_update_batch(const BatchVec<R> *tab, long long n, int B, cudaStream_t s);
+template <typename R>
+void cg_finalize_alpha_batch(const BatchVec<R> *tab, int nparts, int B, cudaStream_t s);
+template <typename R>
+void cg_finalize_beta_batch(const BatchVec<R> *tab, int nparts, int B, cudaStream_t s);
 // FP64 dot of a with b over n entries into *out_device (deterministic)
 template <typename Ra, typename Rb>
 void dot_device(const Ra *a, const Rb *b, long long n, double *partial, double *out,

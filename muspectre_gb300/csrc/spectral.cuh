@@ -185,6 +185,18 @@ template <int D, int TK, typename R> struct TangentLocal {
 };
 
 // ------------------------------------------------------------ pass "last"
+// Per-problem pointers of a batched launch: problem b = blockIdx.y of a grid that
+// covers a batch of same-shape RVEs (or right-hand sides) in one launch per stage.
+template <typename R> struct ProblemPtrs {
+  typename V2<R>::T *spec;
+  const CGState *st;
+  const R *r;
+  R *p;
+  R *Ap;
+  double *partial;
+  TangentData<R> td;
+};
+
 template <typename R> struct LastArgs {
   AxisPlanD<R> ap;
   int L, H, G, ncomp;
@@ -199,13 +211,27 @@ template <typename R> struct LastArgs {
   R *Ap;
   double *partial;
   TangentData<R> td;
+  const ProblemPtrs<R> *batch;  // null: a single problem
+  __device__ __forceinline__ void bind() {
+    if (!batch) return;
+    const ProblemPtrs<R> &q = batch[blockIdx.y];
+    spec = q.spec;
+    st = q.st;
+    r = q.r;
+    p = q.p;
+    Ap = q.Ap;
+    partial = q.partial;
+    td = q.td;
+  }
 };
 
 // forward: real rows -> half spectra.  D is the tensor dimension for the tangent
 // prologues (0 for PRO_PLAIN).
 template <typename R, int PRO, int D, int TK>
-__global__ void __launch_bounds__(kPassThreads) k_last_fwd(const LastArgs<R> a) {
+__global__ void __launch_bounds__(kPassThreads) k_last_fwd(const LastArgs<R> a0) {
   using T = typename V2<R>::T;
+  LastArgs<R> a = a0;
+  a.bind();
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T *buf = reinterpret_cast<T *>(smem_raw);
   if (PRO == PRO_CG && !a.st->active) return;
@@ -303,8 +329,10 @@ __global__ void __launch_bounds__(kPassThreads) k_last_fwd(const LastArgs<R> a) 
 // inverse: half spectra -> real rows.  PLAIN writes out = scale*x; CG writes Ap
 // and the block sums of p.Ap.
 template <typename R, int EPI, int D>
-__global__ void __launch_bounds__(kPassThreads) k_last_inv(const LastArgs<R> a) {
+__global__ void __launch_bounds__(kPassThreads) k_last_inv(const LastArgs<R> a0) {
   using T = typename V2<R>::T;
+  LastArgs<R> a = a0;
+  a.bind();
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T *buf = reinterpret_cast<T *>(smem_raw);
   if (EPI == EPI_CG && !a.st->active) return;
@@ -385,13 +413,19 @@ template <typename R> struct AxisArgs {
   long long se, inner, sb;
   typename V2<R>::T *spec;
   const CGState *st;
+  const ProblemPtrs<R> *batch;
 };
 
 template <typename R, bool INV>
-__global__ void __launch_bounds__(kPassThreads) k_axis(const AxisArgs<R> a) {
+__global__ void __launch_bounds__(kPassThreads) k_axis(const AxisArgs<R> a0) {
   using T = typename V2<R>::T;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T *buf = reinterpret_cast<T *>(smem_raw);
+  AxisArgs<R> a = a0;
+  if (a0.batch) {
+    a.spec = a0.batch[blockIdx.y].spec;
+    a.st = a0.batch[blockIdx.y].st;
+  }
   if (a.st && !a.st->active) return;
   const int tile = blockIdx.x % a.ntiles;
   const long long batch = blockIdx.x / a.ntiles;
@@ -440,13 +474,19 @@ template <typename R> struct GreenArgs {
   int nyq0, nyq1, nyq2;
   R norm;
   const CGState *st;
+  const ProblemPtrs<R> *batch;
 };
 
 template <typename R, int MODE, int D>
-__global__ void __launch_bounds__(kPassThreads) k_green(const GreenArgs<R> a) {
+__global__ void __launch_bounds__(kPassThreads) k_green(const GreenArgs<R> a0) {
   using T = typename V2<R>::T;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T *buf = reinterpret_cast<T *>(smem_raw);
+  GreenArgs<R> a = a0;
+  if (a0.batch) {
+    a.spec = a0.batch[blockIdx.y].spec;
+    a.st = a0.batch[blockIdx.y].st;
+  }
   if (a.st && !a.st->active) return;
   const int Tt = a.T, nc = a.ncomp, n0 = a.n0;
   const int P = nc * Tt;

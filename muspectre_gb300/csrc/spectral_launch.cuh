@@ -124,21 +124,21 @@ template <typename R> LastArgs<R> last_args(Spectral &sp, const Cfg &c) {
 }
 
 template <typename R, int PRO, int D, int TK>
-void launch_fwd(const LastArgs<R> &a, const Cfg &c, cudaStream_t s) {
+void launch_fwd(const LastArgs<R> &a, const Cfg &c, cudaStream_t s, int B = 1) {
   auto k = k_last_fwd<R, PRO, D, TK>;
   allow_smem(k);
-  k<<<c.blocks, c.threads, c.smem, s>>>(a);
+  k<<<dim3(c.blocks, B), c.threads, c.smem, s>>>(a);
   MUSG_CHECK_LAUNCH();
 }
 
 template <typename R, int PRO>
-void dispatch_fwd(int dim, int tk, const LastArgs<R> &a, const Cfg &c, cudaStream_t s) {
+void dispatch_fwd(int dim, int tk, const LastArgs<R> &a, const Cfg &c, cudaStream_t s, int B = 1) {
   if (PRO == PRO_PLAIN) {
-    launch_fwd<R, PRO_PLAIN, 0, TK_PLAIN>(a, c, s);
+    launch_fwd<R, PRO_PLAIN, 0, TK_PLAIN>(a, c, s, B);
     return;
   }
 #define MUSG_FWD_CASE(DD, TT) \
-  if (dim == DD && tk == TT) { launch_fwd<R, PRO, DD, TT>(a, c, s); return; }
+  if (dim == DD && tk == TT) { launch_fwd<R, PRO, DD, TT>(a, c, s, B); return; }
   MUSG_FWD_CASE(2, TK_SMALL) MUSG_FWD_CASE(2, TK_FINITE) MUSG_FWD_CASE(2, TK_KPRIME) MUSG_FWD_CASE(2, TK_MIXED)
   MUSG_FWD_CASE(3, TK_SMALL) MUSG_FWD_CASE(3, TK_FINITE) MUSG_FWD_CASE(3, TK_KPRIME) MUSG_FWD_CASE(3, TK_MIXED)
 #undef MUSG_FWD_CASE
@@ -146,15 +146,16 @@ void dispatch_fwd(int dim, int tk, const LastArgs<R> &a, const Cfg &c, cudaStrea
 }
 
 template <typename R, int EPI, int D>
-void launch_inv(const LastArgs<R> &a, const Cfg &c, cudaStream_t s) {
+void launch_inv(const LastArgs<R> &a, const Cfg &c, cudaStream_t s, int B = 1) {
   auto k = k_last_inv<R, EPI, D>;
   allow_smem(k);
-  k<<<c.blocks, c.threads, c.smem, s>>>(a);
+  k<<<dim3(c.blocks, B), c.threads, c.smem, s>>>(a);
   MUSG_CHECK_LAUNCH();
 }
 
 template <typename R>
-void run_axis(Spectral &sp, bool inv, const CGState *st, cudaStream_t s) {
+void run_axis(Spectral &sp, bool inv, const CGState *st, cudaStream_t s, const ProblemPtrs<R> *batch = nullptr,
+              int B = 1) {
   // 3-D only: pencils along axis 1 of [c][k0][k1][k2h]
   const long long inner = sp.g.nh;
   const long long nbatch = (long long)sp.ncomp * sp.g.n[0];
@@ -169,20 +170,22 @@ void run_axis(Spectral &sp, bool inv, const CGState *st, cudaStream_t s) {
   a.sb = (long long)sp.g.n[1] * sp.g.nh;
   a.spec = spec_of<R>(sp);
   a.st = st;
+  a.batch = batch;
   if (inv) {
     auto k = k_axis<R, true>;
     allow_smem(k);
-    k<<<c.blocks, c.threads, c.smem, s>>>(a);
+    k<<<dim3(c.blocks, B), c.threads, c.smem, s>>>(a);
   } else {
     auto k = k_axis<R, false>;
     allow_smem(k);
-    k<<<c.blocks, c.threads, c.smem, s>>>(a);
+    k<<<dim3(c.blocks, B), c.threads, c.smem, s>>>(a);
   }
   MUSG_CHECK_LAUNCH();
 }
 
 template <typename R>
-void run_green(Spectral &sp, int mode, const CGState *st, cudaStream_t s) {
+void run_green(Spectral &sp, int mode, const CGState *st, cudaStream_t s, const ProblemPtrs<R> *batch = nullptr,
+               int B = 1) {
   const int dim = sp.g.dim;
   const long long Rr = sp.g.nk / sp.g.n[0];
   const Cfg c = green_cfg<R>(sp, Rr);
@@ -205,11 +208,12 @@ void run_green(Spectral &sp, int mode, const CGState *st, cudaStream_t s) {
   a.nyq2 = dim == 3 ? nyq(2) : -1;
   a.norm = R(1.0 / (double)sp.g.npx);
   a.st = st;
+  a.batch = batch;
 #define MUSG_GREEN(MODE, DD)                                     \
   {                                                              \
     auto k = k_green<R, MODE, DD>;                               \
     allow_smem(k);                                               \
-    k<<<c.blocks, c.threads, c.smem, s>>>(a);                 \
+    k<<<dim3(c.blocks, B), c.threads, c.smem, s>>>(a);        \
   }
   if (mode == GM_FWD) MUSG_GREEN(GM_FWD, 2)
   else if (mode == GM_INV) MUSG_GREEN(GM_INV, 2)
@@ -300,6 +304,25 @@ int cg_operator(Spectral &sp, int tkind, const TangentData<R> &td, const CGState
   if (sp.g.dim == 2) launch_inv<R, EPI_CG, 2>(a, c, s);
   else launch_inv<R, EPI_CG, 3>(a, c, s);
   mark();
+  return c.blocks;
+}
+
+static_assert(sizeof(ProblemPtrs<float>) == sizeof(ProblemPtrsHost) &&
+                  sizeof(ProblemPtrs<double>) == sizeof(ProblemPtrsHost),
+              "host image of the batch table");
+
+template <typename R>
+int cg_operator_batch(Spectral &sp, int tkind, const ProblemPtrs<R> *tab, int B, cudaStream_t s) {
+  const int gm = green_mode_of(sp);
+  const Cfg c = last_cfg<R>(sp);
+  LastArgs<R> a = last_args<R>(sp, c);
+  a.batch = tab;
+  dispatch_fwd<R, PRO_CG>(sp.g.dim, tkind, a, c, s, B);
+  if (sp.g.dim == 3) run_axis<R>(sp, false, nullptr, s, tab, B);
+  run_green<R>(sp, gm, nullptr, s, tab, B);
+  if (sp.g.dim == 3) run_axis<R>(sp, true, nullptr, s, tab, B);
+  if (sp.g.dim == 2) launch_inv<R, EPI_CG, 2>(a, c, s, B);
+  else launch_inv<R, EPI_CG, 3>(a, c, s, B);
   return c.blocks;
 }
 
@@ -394,6 +417,7 @@ template <typename R> void spectral_autotune(Spectral &sp, cudaStream_t s, int e
                               R *, R *, double *, cudaStream_t, cudaEvent_t *);                    \
   template void tangent_operator<R>(Spectral &, int, const TangentData<R> &, const R *, R *,       \
                                     cudaStream_t);                                                 \
-  template void spectral_autotune<R>(Spectral &, cudaStream_t, int);
+  template void spectral_autotune<R>(Spectral &, cudaStream_t, int);                               \
+  template int cg_operator_batch<R>(Spectral &, int, const ProblemPtrs<R> *, int, cudaStream_t);
 
 }  // namespace musg

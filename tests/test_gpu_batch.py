@@ -1,0 +1,63 @@
+"""Batched solves: every cell of a batch gets exactly the results of a solo
+newton_cg on it (the batched kernels run the same arithmetic per problem in the same
+order), in FP64 and in mixed precision, and a failing cell leaves the others
+untouched."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope='module')
+def mu():
+    import muspectre_gb300 as m
+    if m.device_count() < 1:
+        pytest.fail('no CUDA device visible')
+    return m
+
+
+def _cells(mu, n, seeds, form='finite'):
+    from muspectre_gb300 import workloads
+    out = []
+    for s in seeds:
+        w = workloads.spheres(n, nsph=5, seed=s)
+        out.append((workloads.build_spheres_cell(mu, w, flags=mu.FFT_PlanFlags.estimate), w))
+    return out
+
+
+@pytest.mark.parametrize('precision', ['fp64', 'mixed'])
+def test_batch_equals_solo(mu, precision):
+    cells = _cells(mu, 24, [1, 2, 3])
+    load = cells[0][1]['load']
+    batch = mu.batch.BatchSolver([c for c, _ in cells], 1e-8, 2000, precision=precision)
+    rb = batch.newton_cg(load, 1e-6, 0.0)
+    for (c, w), res in zip(cells, rb):
+        solo_cell = _cells(mu, 24, [w['seed']])[0][0]
+        rs = mu.solvers.newton_cg(solo_cell, load, mu.solvers.SolverCG(solo_cell, 1e-8, 2000, precision=precision),
+                                  1e-6, 0.0)
+        r = res[0]
+        assert r.success and rs.success
+        assert (r.nb_it, r.nb_fev) == (rs.nb_it, rs.nb_fev)
+        assert np.array_equal(r.stress, rs.stress)
+        assert np.array_equal(c.get_strain(), solo_cell.get_strain())
+
+
+def test_batch_load_path_and_failure(mu):
+    """Two load steps per cell with different loads; a cell given maxiter too small
+    to converge is not part of this check -- instead one batch uses maxiter 1 and
+    every cell reports the ConvergenceError message."""
+    cells = _cells(mu, 16, [4, 5])
+    loads = np.zeros((2, 2, 3, 3))
+    loads[0, :, 0, 0] = [0.01, 0.02]
+    loads[1, :, 1, 1] = [0.005, 0.01]
+    rb = mu.batch.BatchSolver([c for c, _ in cells], 1e-8, 2000).newton_cg(loads, 1e-6, 0.0)
+    for k, ((c, w), res) in enumerate(zip(cells, rb)):
+        solo = _cells(mu, 16, [w['seed']])[0][0]
+        rs = mu.solvers.newton_cg(solo, list(loads[k]), mu.solvers.SolverCG(solo, 1e-8, 2000), 1e-6, 0.0)
+        for a, b in zip(res, rs):
+            assert (a.nb_it, a.nb_fev) == (b.nb_it, b.nb_fev)
+            assert np.array_equal(a.stress, b.stress)
+    cells = _cells(mu, 16, [6, 7])
+    rb = mu.batch.BatchSolver([c for c, _ in cells], 1e-8, 1).newton_cg(cells[0][1]['load'], 1e-6, 0.0)
+    for res in rb:
+        assert not res[0].success and 'not converged' in res[0].message

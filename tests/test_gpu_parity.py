@@ -472,3 +472,28 @@ def test_autotuned_shapes_same_results(mu):
     assert (a.nb_it, a.nb_fev) == (b.nb_it, b.nb_fev)
     assert rel(a.grad, b.grad) < 1e-12
     assert all(t[0] in (128, 256, 512) for t in tb['fp64'].values())
+
+
+@pytest.mark.parametrize('logm', ['projector', 'spectral'])
+def test_hep1_uniaxial_config_status(mu, logm):
+    """BASELINE config 4 restated at 15³ (two HEP1 phases on a periodic Voronoi,
+    uniaxial F11 ramp).  The reference method does not solve it: with the projector
+    logm (eigen_tools.hh:209-322) the uniform first step has repeated eigenvalues and
+    gives NaN; with the spectral logm the CG diverges on the j-independent
+    Kirchhoff->PK1 tangent (materials_toolbox.hh:374-410).  Parity is the same
+    ConvergenceError on the GPU as in the oracle."""
+    from muspectre_gb300 import workloads
+    w = workloads.voronoi(n=15, nseeds=8, nsteps=4)
+    ocell = o.Cell(w['res'], w['lengths'], o.FINITE_STRAIN)
+    gcell = mu.Cell(w['res'], w['lengths'], mu.Formulation.finite_strain)
+    for ph, mask in (('A', w['phaseA']), ('B', ~w['phaseA'])):
+        p = w[ph]
+        m = ocell.add_material(o.MaterialHyperElastoPlastic1(ph, 3, p['E'], p['nu'], p['tau_y0'], p['H'],
+                                                             logm_mode=logm))
+        m.pixels = list(np.flatnonzero(mask))
+        mu.material.MaterialHyperElastoPlastic1_3d.make(gcell, ph, p['E'], p['nu'], p['tau_y0'], p['H'],
+                                                       logm=logm).add_pixels(mask)
+    with pytest.raises(o.ConvergenceError):
+        o.newton_cg(ocell, w['steps'], o.SolverCG(ocell, 1e-8, 300), 1e-6, 0.0, 0)
+    with pytest.raises(mu.ConvergenceError):
+        mu.solvers.newton_cg(gcell, w['steps'], mu.solvers.SolverCG(gcell, 1e-8, 300), 1e-6, 0.0)

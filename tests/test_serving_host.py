@@ -1,0 +1,57 @@
+"""Host logic of the request server (no GPU): admission by HBM budget, same-shape
+batching, memory returned on completion, the config-5 request generator."""
+import numpy as np
+
+from muspectre_gb300 import serving
+from muspectre_gb300.cell import Formulation
+
+
+def _req(rid, n, hep=False):
+    d = 2
+    phase = np.zeros(n * n, dtype=np.int64)
+    mats = [('hep1', (1e9, .3, 1e6, 1e7))] if hep else [('le1', (1e9, .3))]
+    return serving.Request(rid, [n, n], int(Formulation.finite_strain), phase, mats, [np.eye(d) * 0.01])
+
+
+def test_estimate_bytes_grows():
+    a = serving.estimate_bytes([64, 64], Formulation.small_strain, False)
+    b = serving.estimate_bytes([128, 128], Formulation.small_strain, False)
+    c = serving.estimate_bytes([128, 128], Formulation.finite_strain, True)
+    assert 0 < a < b < c
+    assert serving.estimate_bytes([64] * 3, 0, False, 'fp64') != serving.estimate_bytes([64] * 3, 0, False, 'mixed')
+
+
+def test_admission_budget_and_batching():
+    fp = serving.estimate_bytes([64, 64], Formulation.finite_strain, False)
+    srv = serving.Server(hbm_budget_bytes=int(2.5 * fp), lanes=2, max_batch=4)
+    for rid, n in enumerate([64, 64, 96, 64, 64]):
+        srv.queue.append(_req(rid, n))
+    g1, used1 = srv._take()
+    assert [r.rid for r in g1] == [0, 1]          # same shape, two fit the budget
+    assert srv.in_use == used1 <= srv.budget
+    g2, used2 = srv._take()                       # 96^2 does not fit next to two 64^2
+    assert g2 is None or srv.in_use <= srv.budget
+    srv.in_use -= used1                           # first group completes
+    g3, used3 = srv._take()
+    assert g3 is not None and srv.in_use <= srv.budget
+
+
+def test_oversized_request_admitted_alone():
+    srv = serving.Server(hbm_budget_bytes=1, lanes=1)
+    srv.queue.append(_req(0, 64))
+    g, used = srv._take()                          # an idle server admits it anyway
+    assert g is not None and len(g) == 1 and srv.in_use == used
+
+
+def test_c5_generator_ranges():
+    for seed in range(40):
+        r = serving.c5_request(seed, seed, small=True)
+        d = len(r.res)
+        n = r.res[0]
+        assert (d == 2 and 64 <= n <= 160) or (d == 3 and 32 <= n <= 40)
+        assert serving._smooth235(n)
+        if any(m[0] == 'hep1' for m in r.materials):
+            assert r.formulation == Formulation.finite_strain
+            assert 1 <= len(r.steps) <= 10
+        for s in r.steps:
+            assert np.allclose(s, s.T) and np.all(np.abs(s) <= 0.02 + 1e-12)
