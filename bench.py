@@ -277,13 +277,6 @@ def main():
     value = world * args.steps / (t_ms / 1000.0)
     stress_mixed = None
 
-    if args.only == 'mixed':
-        if rank == 0:
-            print(json.dumps({'metric': 'RVE solves/s (mixed only)', 'value': value, 'unit': 'solves/s',
-                              'ms_per_step': t_ms / args.steps, 'cg_iters_per_solve': cg_per_solve,
-                              'gpu_launches': launches}), flush=True)
-        return
-
     # per-kernel profile of one CG iteration (mixed) + roofline
     prof = mixed.profile(5)
     peak, peak_kind = measured_peaks()
@@ -302,6 +295,14 @@ def main():
             'iteration_ms': tot,
             'iteration_gbs': sum(v['bytes'] for v in kern.values()) / (tot * 1e-3) / 1e9 if tot else None,
             'kernels': kern}
+    if args.only == 'mixed':
+        if rank == 0:
+            print(json.dumps({'metric': 'RVE solves/s (mixed only)', 'value': value, 'unit': 'solves/s',
+                              'ms_per_step': t_ms / args.steps, 'cg_iters_per_solve': cg_per_solve,
+                              'gpu_launches': launches, 'launch_shapes': cell.tuning(),
+                              'kernels': {k: [round(v['ms'] * 1e3, 1), round(v['gbs'] or 0)] for k, v in kern.items()},
+                              'iteration_us': round(tot * 1e3, 1)}), flush=True)
+        return
 
     # ---------------- FP64 method on the same input
     fp64_lat = []

@@ -133,6 +133,11 @@ int musg_cell_evaluate_stress_tangent(musg_cell *cell, double *stress_out,
 int musg_cell_apply_projection(musg_cell *cell, double *vec);
 /* Cell::evaluate_projected_directional_stiffness (cell_base.cc:150-192) */
 int musg_cell_directional_stiffness(musg_cell *cell, const double *dF, double *dP);
+/* G(K:dF) through the kernels of one CG iteration (the operator SolverCG applies) in
+ * the given precision (MUSG_PRECISION_FP64 or _MIXED = FP32 operator).  No reference
+ * counterpart: it exposes the operator of the mixed-precision path for checking.
+ * Needs an evaluated tangent; host arrays as in musg_cell_directional_stiffness. */
+int musg_cell_cg_operator(musg_cell *cell, int precision, const double *dF, double *dP);
 /* Cell::save_history_variables (cell_base.cc:458-462) */
 int musg_cell_save_history_variables(musg_cell *cell);
 

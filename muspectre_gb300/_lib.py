@@ -70,6 +70,7 @@ _SIGNATURES = {
     'musg_cell_evaluate_stress_tangent': (C.c_int, [_P, _D, _D]),
     'musg_cell_apply_projection': (C.c_int, [_P, _D]),
     'musg_cell_directional_stiffness': (C.c_int, [_P, _D, _D]),
+    'musg_cell_cg_operator': (C.c_int, [_P, C.c_int, _D, _D]),
     'musg_cell_save_history_variables': (C.c_int, [_P]),
     'musg_solver_cg_create': (C.c_int, [_P, C.c_double, C.c_uint, C.c_int, C.c_int, C.POINTER(_P)]),
     'musg_solver_destroy': (C.c_int, [_P]),

@@ -251,6 +251,17 @@ class CellBase:
         L.check(L.lib().musg_cell_directional_stiffness(self._h, L.dptr(v), L.dptr(out)))
         return out
 
+    def cg_operator(self, dF, precision='fp64'):
+        """G(K:dF) for a (D², N) array through the kernels of one CG iteration, in FP64
+        or in the FP32 operator of the mixed-precision solver (an extension for
+        checking the mixed path; needs an evaluated tangent)."""
+        self.initialise()
+        v = self._as_field(dF)
+        out = np.empty(self.nb_dof)
+        prec = {'fp64': L.PRECISION_FP64, 'mixed': L.PRECISION_MIXED}[precision]
+        L.check(L.lib().musg_cell_cg_operator(self._h, prec, L.dptr(v), L.dptr(out)))
+        return self._to_array(out)
+
     def save_history_variables(self):
         L.check(L.lib().musg_cell_save_history_variables(self._h))
 

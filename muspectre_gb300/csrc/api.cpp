@@ -126,7 +126,8 @@ struct musg_cell {
   bool own_stream = false;
   std::vector<Material> materials;
   Spectral sp;
-  int tkind = TK_SMALL;
+  int tkind = TK_SMALL, tkind32 = TK_SMALL;  // CG operator kind of the FP64 / FP32 path
+  template <typename R> int tk() const { return sizeof(R) == 4 ? tkind32 : tkind; }
   int hep_cur = 0;
   bool has_le2 = false, has_hep = false;
   // device fields (FP64 component planes)
@@ -266,6 +267,8 @@ struct musg_cell {
     else if (has_hep && any_le) tkind = TK_MIXED;
     else if (has_hep) tkind = TK_KPRIME;
     else tkind = TK_FINITE;
+    // the FP32 operator rebuilds S from F where the law allows (not LE2: eigenstrain)
+    tkind32 = (tkind == TK_FINITE && !has_le2) ? TK_FISO : tkind;
     mat.alloc(npx);
     MUSG_CUDA(cudaMemcpy(mat.p, hmat.data(), npx, cudaMemcpyHostToDevice));
     params.alloc(hp.size() * sizeof(MatParams));
@@ -368,7 +371,7 @@ struct musg_cell {
     a.cur = hep_cur;
     a.S64 = S64.as<double>();
     a.Kp64 = Kp64.as<double>();
-    a.S32 = S32.as<float>();
+    a.S32 = tkind32 == TK_FISO ? nullptr : S32.as<float>();
     a.Kp32 = Kp32.as<float>();
     a.Fc32 = Fc32.as<float>();
     a.Fc64 = Fc64.as<double>();
@@ -485,13 +488,13 @@ struct musg_solver {
     CGState *d = st.as<CGState>();
     double *part = c.partial.as<double>();
     const TangentData<R> td = c.tangent<R>();
-    const int nop = cg_operator<R>(c.sp, c.tkind, td, d, r.as<R>(), p.as<R>(), Ap.as<R>(), part, s, ev);
+    const int nop = cg_operator<R>(c.sp, c.tk<R>(), td, d, r.as<R>(), p.as<R>(), Ap.as<R>(), part, s, ev);
     int k = c.dim == 3 ? 5 : 3;
     cg_finalize_alpha(d, part, nop, s);
     if (ev) MUSG_CUDA(cudaEventRecord(ev[++k], s));
     cg_update<R>(d, x.as<R>(), r.as<R>(), p.as<R>(), Ap.as<R>(), n, part, s);
     if (ev) MUSG_CUDA(cudaEventRecord(ev[++k], s));
-    cg_finalize_beta(d, part, reduce_blocks(n), s);
+    cg_finalize_beta(d, part, update_blocks(n), s);
     if (ev) MUSG_CUDA(cudaEventRecord(ev[++k], s));
     return k;  // number of kernels
   }
@@ -664,10 +667,10 @@ struct musg_batch {
   template <typename R> void iteration(cudaStream_t s) {
     musg_cell &c0 = *cells[0];
     const long long n = c0.nb_dof();
-    const int nop = cg_operator_batch<R>(c0.sp, c0.tkind, (const ProblemPtrs<R> *)tab_p.p, B(), s);
+    const int nop = cg_operator_batch<R>(c0.sp, c0.tk<R>(), (const ProblemPtrs<R> *)tab_p.p, B(), s);
     cg_finalize_alpha_batch<R>(tab_v.as<BatchVec<R>>(), nop, B(), s);
     cg_update_batch<R>(tab_v.as<BatchVec<R>>(), n, B(), s);
-    cg_finalize_beta_batch<R>(tab_v.as<BatchVec<R>>(), reduce_blocks(n), B(), s);
+    cg_finalize_beta_batch<R>(tab_v.as<BatchVec<R>>(), update_blocks(n), B(), s);
   }
 
   template <typename R> void build_graph() {
@@ -987,6 +990,29 @@ void batch_newton_impl(musg_batch *batch, const double *steps, int nsteps, doubl
 }  // namespace
 
 // ====================================================================== C ABI
+namespace {
+template <typename R> void cg_operator_once(musg_cell &c, const double *dF, double *dP) {
+  const long long n = c.nb_dof();
+  if (c.io2.bytes < c.field_bytes()) c.io2.alloc(c.field_bytes());
+  c.upload_field(dF, c.io2.as<double>());
+  DevBuf r, p, Ap, st;
+  r.alloc((size_t)n * sizeof(R));
+  p.alloc((size_t)n * sizeof(R));
+  Ap.alloc((size_t)n * sizeof(R));
+  st.alloc(sizeof(CGState));
+  // first CG iteration: p = -r, so r = -dF gives p = dF and Ap = G(K:dF)
+  convert<R, double>(r.as<R>(), c.io2.as<double>(), n, -1.0, c.stream);
+  CGState h{};
+  h.maxiter = 1;
+  h.active = 1;
+  MUSG_CUDA(cudaMemcpyAsync(st.p, &h, sizeof(h), cudaMemcpyHostToDevice, c.stream));
+  cg_operator<R>(c.sp, c.tk<R>(), c.tangent<R>(), st.as<CGState>(), r.as<R>(), p.as<R>(), Ap.as<R>(),
+                 c.partial.as<double>(), c.stream);
+  convert<double, R>(c.io2.as<double>(), Ap.as<R>(), n, 1.0, c.stream);
+  c.download_field(c.io2.as<double>(), dP);
+}
+}  // namespace
+
 extern "C" {
 
 const char *musg_last_error(void) { return g_last_error.c_str(); }
@@ -1192,6 +1218,26 @@ int musg_cell_directional_stiffness(musg_cell *cell, const double *dF, double *d
   });
 }
 
+int musg_cell_cg_operator(musg_cell *cell, int precision, const double *dF, double *dP) {
+  return guard([&] {
+    require(cell && dF && dP, MUSG_ERR_ARGUMENT, "null argument");
+    require(precision == MUSG_PRECISION_FP64 || precision == MUSG_PRECISION_MIXED, MUSG_ERR_ARGUMENT,
+            "unknown precision");
+    musg_cell &c = *cell;
+    require(c.tangent_valid, MUSG_ERR_RUNTIME,
+            "currently only implemented for cases where a stiffness matrix exists");
+    if (precision == MUSG_PRECISION_FP64) {
+      cg_operator_once<double>(c, dF, dP);
+      return;
+    }
+    if (!c.need32 || !c.lam32.p) {
+      c.alloc32();
+      c.evaluate(false);  // the FP32 tangent data of the current strain
+    }
+    cg_operator_once<float>(c, dF, dP);
+  });
+}
+
 int musg_cell_save_history_variables(musg_cell *cell) {
   return guard([&] {
     require(cell, MUSG_ERR_ARGUMENT, "null cell");
@@ -1289,7 +1335,7 @@ int musg_batch_create(musg_cell **cells, int nb_cells, double tol, unsigned maxi
       require(cells[b] != nullptr, MUSG_ERR_ARGUMENT, "null cell");
       if (!c.initialised) c.initialise();
       require(c.dim == c0.dim && c.form == c0.form && c.res[0] == c0.res[0] && c.res[1] == c0.res[1] &&
-                  c.res[2] == c0.res[2] && c.flags == c0.flags && c.tkind == c0.tkind,
+                  c.res[2] == c0.res[2] && c.flags == c0.flags && c.tkind == c0.tkind && c.tkind32 == c0.tkind32,
               MUSG_ERR_ARGUMENT, "cells of a batch need the same grid, formulation and material-law kind");
       for (int k = 0; k < b; ++k) require(cells[k] != cells[b], MUSG_ERR_ARGUMENT, "a cell appears twice in a batch");
       auto sv = std::make_unique<musg_solver>();

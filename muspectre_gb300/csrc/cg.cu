@@ -8,6 +8,9 @@
 // fixed order), so a rerun gives bit-identical scalars.  FP32 vectors are
 // accumulated with Neumaier-compensated FP32 sums per thread and FP64 across
 // threads and blocks.
+#include <algorithm>
+#include <cstdint>
+
 #include "spectral.cuh"
 
 namespace musg {
@@ -76,26 +79,77 @@ void cg_init(CGState *st, const double *rhs, R *r, R *x, long long n, double tol
   MUSG_CHECK_LAUNCH();
 }
 
-// x += alpha p, r += alpha Ap, partial sums of r.r
+// x += alpha p, r += alpha Ap, partial sums of r.r.  16-byte vectors (float4 /
+// double2) over one wave of blocks; the scalar tail (n not a multiple of the vector
+// width) goes to block 0.  Solo and batched launches share this body, so a problem
+// gives bit-identical scalars in both.
+template <typename R> struct Vec16;
+template <> struct Vec16<float> { using T = float4; static constexpr int W = 4; };
+template <> struct Vec16<double> { using T = double2; static constexpr int W = 2; };
+
+template <typename R>
+__device__ __forceinline__ double cg_update_body(R alpha, R *__restrict__ x, R *__restrict__ r,
+                                                 const R *__restrict__ p, const R *__restrict__ Ap, long long n) {
+  using V = typename Vec16<R>::T;
+  constexpr int W = Vec16<R>::W;
+  Acc<R> acc;
+  const long long nv = n / W;
+  V *xv = reinterpret_cast<V *>(x);
+  V *rv = reinterpret_cast<V *>(r);
+  const V *pv = reinterpret_cast<const V *>(p);
+  const V *av = reinterpret_cast<const V *>(Ap);
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < nv; i += (long long)gridDim.x * blockDim.x) {
+    V xi = xv[i], ri = rv[i];
+    const V pi = pv[i], ai = av[i];
+    R *xs = reinterpret_cast<R *>(&xi);
+    R *rs = reinterpret_cast<R *>(&ri);
+    const R *ps = reinterpret_cast<const R *>(&pi);
+    const R *as = reinterpret_cast<const R *>(&ai);
+#pragma unroll
+    for (int u = 0; u < W; ++u) {
+      xs[u] += alpha * ps[u];
+      rs[u] = rs[u] + alpha * as[u];
+      acc.add(rs[u] * rs[u]);
+    }
+    xv[i] = xi;
+    rv[i] = ri;
+  }
+  if (blockIdx.x == 0) {
+    for (long long i = nv * W + threadIdx.x; i < n; i += blockDim.x) {
+      x[i] += alpha * p[i];
+      const R v = r[i] + alpha * Ap[i];
+      r[i] = v;
+      acc.add(v * v);
+    }
+  }
+  return block_sum(acc.value());
+}
+
 template <typename R>
 __global__ void k_cg_update(const CGState *__restrict__ st, R *__restrict__ x, R *__restrict__ r,
                             const R *__restrict__ p, const R *__restrict__ Ap, long long n, double *partial) {
   if (!st->active) return;
-  const R alpha = R(st->alpha);
-  Acc<R> acc;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-    x[i] += alpha * p[i];
-    const R rv = r[i] + alpha * Ap[i];
-    r[i] = rv;
-    acc.add(rv * rv);
-  }
-  const double bs = block_sum(acc.value());
+  const double bs = cg_update_body<R>(R(st->alpha), x, r, p, Ap, n);
   if (threadIdx.x == 0) partial[blockIdx.x] = bs;
 }
 
+int update_blocks(long long n) {
+  static int nsm[64] = {0};
+  int dev = 0;
+  MUSG_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) dev = 0;
+  if (nsm[dev] == 0) MUSG_CUDA(cudaDeviceGetAttribute(&nsm[dev], cudaDevAttrMultiProcessorCount, dev));
+  const long long need = (n / 2 + kRedThreads - 1) / kRedThreads;
+  return (int)std::max<long long>(1, std::min<long long>(need, std::min(8LL * nsm[dev], (long long)kRedMaxBlocks)));
+}
+
+inline bool aligned16(const void *q) { return ((uintptr_t)q & 15u) == 0; }
+
 template <typename R>
 void cg_update(const CGState *st, R *x, R *r, const R *p, const R *Ap, long long n, double *partial, cudaStream_t s) {
-  k_cg_update<R><<<reduce_blocks(n), kRedThreads, 0, s>>>(st, x, r, p, Ap, n, partial);
+  if (!(aligned16(x) && aligned16(r) && aligned16(p) && aligned16(Ap)))
+    throw Error(MUSG_ERR_ARGUMENT, "CG vectors must be 16-byte aligned");
+  k_cg_update<R><<<update_blocks(n), kRedThreads, 0, s>>>(st, x, r, p, Ap, n, partial);
   MUSG_CHECK_LAUNCH();
 }
 
@@ -137,15 +191,7 @@ template <typename R>
 __global__ void k_cg_update_b(const BatchVec<R> *tab, long long n) {
   const BatchVec<R> q = tab[blockIdx.y];
   if (!q.st->active) return;
-  const R alpha = R(q.st->alpha);
-  Acc<R> acc;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-    q.x[i] += alpha * q.p[i];
-    const R rv = q.r[i] + alpha * q.Ap[i];
-    q.r[i] = rv;
-    acc.add(rv * rv);
-  }
-  const double bs = block_sum(acc.value());
+  const double bs = cg_update_body<R>(R(q.st->alpha), q.x, q.r, q.p, q.Ap, n);
   if (threadIdx.x == 0) q.partial[blockIdx.x] = bs;
 }
 
@@ -173,7 +219,7 @@ template <typename R> __global__ void k_cg_beta_b(const BatchVec<R> *tab, int np
 }
 
 template <typename R> void cg_update_batch(const BatchVec<R> *tab, long long n, int B, cudaStream_t s) {
-  k_cg_update_b<R><<<dim3(reduce_blocks(n), B), kRedThreads, 0, s>>>(tab, n);
+  k_cg_update_b<R><<<dim3(update_blocks(n), B), kRedThreads, 0, s>>>(tab, n);
   MUSG_CHECK_LAUNCH();
 }
 

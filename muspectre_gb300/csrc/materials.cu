@@ -414,7 +414,7 @@ __global__ void __launch_bounds__(kMatThreads) k_material(const MaterialArgs a, 
   if (finite) {
 #pragma unroll
     for (int c = 0; c < D2; ++c) {
-      if (a.Fc32) store(a.Fc32, c * N + px, F.a[c]);
+      if (a.Fc32) store(a.Fc32, c * N + px, F.a[c] - ((c % (D + 1)) == 0 ? 1.0 : 0.0));  // H = F - I
       if (a.Fc64) store(a.Fc64, c * N + px, F.a[c]);
     }
   }

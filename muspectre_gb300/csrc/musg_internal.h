@@ -88,13 +88,14 @@ enum TangentKind : int {
   TK_FINITE = 2,  // finite strain, isotropic PK2/GL: dP = dF S + F (lam tr(A) I + mu (A + A^T)), A = F^T dF
   TK_KPRIME = 3,  // j-independent Kirchhoff tangent: dP(i,m) = sum_n K'(i,m,n) sum_j dF(j,n)
   TK_MIXED = 4,   // per-pixel choice between TK_FINITE and TK_KPRIME by material law
+  TK_FISO = 5,    // TK_FINITE with S rebuilt from F per application (isotropic LE1/LE3/LE4)
 };
 
 // Device data the CG operator reads (precision R).
 template <typename R> struct TangentData {
   const R *lam = nullptr;   // [npx]
   const R *mu = nullptr;    // [npx]
-  const R *F = nullptr;     // [D*D][npx]  (finite strain)
+  const R *F = nullptr;     // [D*D][npx]  (finite strain): F in FP64, F - I in FP32
   const R *S = nullptr;     // [D*D][npx] PK2 stress (finite strain, isotropic)
   const R *Kp = nullptr;    // [D^3][npx]  (Kirchhoff tangent)
   const uint8_t *mat = nullptr;      // [npx] material index (TK_MIXED)
@@ -188,6 +189,8 @@ template <typename R> void spectral_autotune(Spectral &sp, cudaStream_t s, int e
 
 // ---------------------------------------------------------------- CG kernels (cg.cu)
 int reduce_blocks(long long n);
+// blocks (= partial sums) of cg_update / cg_update_batch for n entries
+int update_blocks(long long n);
 template <typename R>
 void cg_init(CGState *st, const double *rhs, R *r, R *x, long long n, double tol,
              int maxiter, double *partial, double *partial2, cudaStream_t s);

@@ -49,17 +49,19 @@ template <> struct Acc<double> {
   __device__ __forceinline__ double value() const { return s; }
 };
 
-// sum of v over the block, result valid in thread 0
+// sum of v over the block (1-, 2- or 3-D, a whole number of warps), result valid in
+// the thread of linear index 0
 __device__ __forceinline__ double block_sum(double v) {
   __shared__ double red[32];
   for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  const int tid = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
+  const int w = tid >> 5, l = tid & 31;
   __syncthreads();
   if (l == 0) red[w] = v;
   __syncthreads();
   v = 0.0;
   if (w == 0) {
-    const int nw = (blockDim.x + 31) >> 5;
+    const int nw = (blockDim.x * blockDim.y * blockDim.z + 31) >> 5;
     v = (l < nw) ? red[l] : 0.0;
     for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
   }
@@ -140,7 +142,7 @@ __device__ __forceinline__ void tangent_kprime(const R *dF, const R *Kp, R *out)
 // all of a pixel's global loads are in flight together.
 template <int D, int TK, typename R> struct TangentLocal {
   static constexpr int D2 = D * D;
-  static constexpr bool kFinite = (TK == TK_FINITE || TK == TK_MIXED);
+  static constexpr bool kFinite = (TK == TK_FINITE || TK == TK_MIXED || TK == TK_FISO);
   static constexpr bool kKprime = (TK == TK_KPRIME || TK == TK_MIXED);
   int kind;
   R lam, mu;
@@ -155,11 +157,13 @@ template <int D, int TK, typename R> struct TangentLocal {
       mu = td.mu[px];
     }
     if constexpr (kFinite) {
-      if (TK == TK_FINITE || kind == TK_FINITE) {
+      if (TK == TK_FINITE || TK == TK_FISO || kind == TK_FINITE) {
 #pragma unroll
         for (int c = 0; c < D2; ++c) F[c] = td.F[c * npx + px];
+        if constexpr (TK != TK_FISO) {
 #pragma unroll
-        for (int c = 0; c < D2; ++c) S[c] = td.S[c * npx + px];
+          for (int c = 0; c < D2; ++c) S[c] = td.S[c * npx + px];
+        }
       }
     }
     if constexpr (kKprime) {
@@ -170,10 +174,42 @@ template <int D, int TK, typename R> struct TangentLocal {
     }
   }
 
-  __device__ __forceinline__ void apply(const R *in, R *out) const {
+  // the FP32 copy of F holds H = F - I (exact where F is near I); form F, and for
+  // TK_FISO the PK2 stress S = lam tr(E) I + 2 mu E with E = (H + H^T + H^T H)/2
+  // (materials_toolbox.hh:139-148, 661-663)
+  __device__ __forceinline__ void finish() {
+    if constexpr (kFinite && sizeof(R) == 4) {
+      if constexpr (TK == TK_FISO) {
+        R E[D2];
+        R tr = R(0);
+#pragma unroll
+        for (int j = 0; j < D; ++j)
+#pragma unroll
+          for (int i = 0; i < D; ++i) {
+            R hh = R(0);
+#pragma unroll
+            for (int k = 0; k < D; ++k) hh += F[k + D * i] * F[k + D * j];
+            E[i + D * j] = R(0.5) * (F[i + D * j] + F[j + D * i] + hh);
+          }
+#pragma unroll
+        for (int i = 0; i < D; ++i) tr += E[i + D * i];
+#pragma unroll
+        for (int j = 0; j < D; ++j)
+#pragma unroll
+          for (int i = 0; i < D; ++i) S[i + D * j] = R(2) * mu * E[i + D * j] + (i == j ? lam * tr : R(0));
+      }
+      if (TK != TK_MIXED || kind == TK_FINITE) {
+#pragma unroll
+        for (int i = 0; i < D; ++i) F[i + D * i] += R(1);
+      }
+    }
+  }
+
+  __device__ __forceinline__ void apply(const R *in, R *out) {
+    finish();
     if constexpr (TK == TK_SMALL) {
       tangent_small<D, R>(in, lam, mu, out);
-    } else if constexpr (TK == TK_FINITE) {
+    } else if constexpr (TK == TK_FINITE || TK == TK_FISO) {
       tangent_finite<D, R>(in, F, S, lam, mu, out);
     } else if constexpr (TK == TK_KPRIME) {
       tangent_kprime<D, R>(in, Kp, out);
@@ -464,6 +500,63 @@ __global__ void __launch_bounds__(kPassThreads) k_axis(const AxisArgs<R> a0) {
   }
 }
 
+// ------------------------------------------------------------ Green operators
+// unit wave vector of k-point (xi0[e], xi1[k1], xi2[k2]); false where the operator
+// is zero (the zero mode, and every Nyquist index under the even-grid extension)
+template <int D, typename R>
+__device__ __forceinline__ bool unit_xi(R *xi, int e, int k1, int k2, int nyq0, int nyq1, int nyq2) {
+  if ((e == 0 && k1 == 0 && k2 == 0) || e == nyq0 || k1 == nyq1 || (D == 3 && k2 == nyq2)) return false;
+  R n2 = R(0);
+#pragma unroll
+  for (int d = 0; d < D; ++d) n2 += xi[d] * xi[d];
+  const R inv = R(1) / sqrt(n2);
+#pragma unroll
+  for (int d = 0; d < D; ++d) xi[d] *= inv;
+  return true;
+}
+
+// finite strain, one row i of f: f_i. <- (f_i. xi) xi^T / N
+// (projection_finite_strain_fast.cc:79-85)
+template <int D, typename T, typename R>
+__device__ __forceinline__ void green_finite_row(T *row, const R *xi, R norm) {
+  T fx = T{R(0), R(0)};
+#pragma unroll
+  for (int j = 0; j < D; ++j) {
+    fx.x += row[j].x * xi[j];
+    fx.y += row[j].y * xi[j];
+  }
+#pragma unroll
+  for (int j = 0; j < D; ++j) row[j] = T{fx.x * xi[j] * norm, fx.y * xi[j] * norm};
+}
+
+// small strain: Ghat f = 1/2 (xi a^T + a xi^T) - xi xi^T (xi^T f xi) with a = (f + f^T) xi,
+// the contraction of the operator of projection_small_strain.cc:64-77 with f, / N
+template <int D, typename T, typename R>
+__device__ __forceinline__ void green_small(const T *f, T *o, const R *xi, R norm) {
+  T av[D];
+  T s = T{R(0), R(0)};
+#pragma unroll
+  for (int i = 0; i < D; ++i) {
+    T v = T{R(0), R(0)};
+#pragma unroll
+    for (int j = 0; j < D; ++j) {
+      v.x += (f[i + D * j].x + f[j + D * i].x) * xi[j];
+      v.y += (f[i + D * j].y + f[j + D * i].y) * xi[j];
+      s.x += xi[i] * f[i + D * j].x * xi[j];
+      s.y += xi[i] * f[i + D * j].y * xi[j];
+    }
+    av[i] = v;
+  }
+#pragma unroll
+  for (int j = 0; j < D; ++j)
+#pragma unroll
+    for (int i = 0; i < D; ++i) {
+      const R xx = xi[i] * xi[j];
+      o[i + D * j] = T{(R(0.5) * (xi[i] * av[j].x + av[i].x * xi[j]) - xx * s.x) * norm,
+                       (R(0.5) * (xi[i] * av[j].y + av[i].y * xi[j]) - xx * s.y) * norm};
+    }
+}
+
 // ------------------------------------------------------------ pass "green"
 template <typename R> struct GreenArgs {
   AxisPlanD<R> ap;
@@ -536,59 +629,26 @@ __global__ void __launch_bounds__(kPassThreads) k_green(const GreenArgs<R> a0) {
       xi[0] = a.xi0[e];
       xi[1] = a.xi1[k1];
       if (D == 3) xi[D - 1] = a.xi2[k2];
-      bool zero = (e == 0 && k1 == 0 && k2 == 0) || e == a.nyq0 || k1 == a.nyq1 || (D == 3 && k2 == a.nyq2);
       T f[D2];
 #pragma unroll
       for (int c = 0; c < D2; ++c) f[c] = cur[e * P + c * Tt + t];
       T o[D2];
-      if (zero) {
+      if (!unit_xi<D>(xi, e, k1, k2, a.nyq0, a.nyq1, a.nyq2)) {
 #pragma unroll
         for (int c = 0; c < D2; ++c) o[c] = T{R(0), R(0)};
       } else {
-        R n2 = R(0);
-#pragma unroll
-        for (int d = 0; d < D; ++d) n2 += xi[d] * xi[d];
-        const R inv = R(1) / sqrt(n2);
-#pragma unroll
-        for (int d = 0; d < D; ++d) xi[d] *= inv;
         if (MODE == GM_FINITE) {
-          // f <- (f xi) xi^T   (projection_finite_strain_fast.cc:79-85)
 #pragma unroll
           for (int i = 0; i < D; ++i) {
-            T fx = T{R(0), R(0)};
+            T row[D];
 #pragma unroll
-            for (int j = 0; j < D; ++j) {
-              fx.x += f[i + D * j].x * xi[j];
-              fx.y += f[i + D * j].y * xi[j];
-            }
+            for (int j = 0; j < D; ++j) row[j] = f[i + D * j];
+            green_finite_row<D>(row, xi, a.norm);
 #pragma unroll
-            for (int j = 0; j < D; ++j) o[i + D * j] = T{fx.x * xi[j] * a.norm, fx.y * xi[j] * a.norm};
+            for (int j = 0; j < D; ++j) o[i + D * j] = row[j];
           }
         } else {
-          // Ghat f = 1/2 (xi a^T + a xi^T) - xi xi^T (xi^T f xi),  a = (f + f^T) xi
-          // (the contraction of projection_small_strain.cc:64-77 with f)
-          T av[D];
-          T s = T{R(0), R(0)};
-#pragma unroll
-          for (int i = 0; i < D; ++i) {
-            T v = T{R(0), R(0)};
-#pragma unroll
-            for (int j = 0; j < D; ++j) {
-              v.x += (f[i + D * j].x + f[j + D * i].x) * xi[j];
-              v.y += (f[i + D * j].y + f[j + D * i].y) * xi[j];
-              s.x += xi[i] * f[i + D * j].x * xi[j];
-              s.y += xi[i] * f[i + D * j].y * xi[j];
-            }
-            av[i] = v;
-          }
-#pragma unroll
-          for (int j = 0; j < D; ++j)
-#pragma unroll
-            for (int i = 0; i < D; ++i) {
-              const R xx = xi[i] * xi[j];
-              o[i + D * j] = T{(R(0.5) * (xi[i] * av[j].x + av[i].x * xi[j]) - xx * s.x) * a.norm,
-                               (R(0.5) * (xi[i] * av[j].y + av[i].y * xi[j]) - xx * s.y) * a.norm};
-            }
+          green_small<D>(f, o, xi, a.norm);
         }
       }
 #pragma unroll

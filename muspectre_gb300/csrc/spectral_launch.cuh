@@ -7,6 +7,7 @@
 #include <set>
 
 #include "spectral.cuh"
+#include "spectral_reg.cuh"
 
 namespace musg {
 
@@ -141,6 +142,9 @@ void dispatch_fwd(int dim, int tk, const LastArgs<R> &a, const Cfg &c, cudaStrea
   if (dim == DD && tk == TT) { launch_fwd<R, PRO, DD, TT>(a, c, s, B); return; }
   MUSG_FWD_CASE(2, TK_SMALL) MUSG_FWD_CASE(2, TK_FINITE) MUSG_FWD_CASE(2, TK_KPRIME) MUSG_FWD_CASE(2, TK_MIXED)
   MUSG_FWD_CASE(3, TK_SMALL) MUSG_FWD_CASE(3, TK_FINITE) MUSG_FWD_CASE(3, TK_KPRIME) MUSG_FWD_CASE(3, TK_MIXED)
+  if (sizeof(R) == 4) {
+    MUSG_FWD_CASE(2, TK_FISO) MUSG_FWD_CASE(3, TK_FISO)
+  }
 #undef MUSG_FWD_CASE
   throw Error(MUSG_ERR_ARGUMENT, "unsupported tangent kind");
 }
@@ -153,12 +157,163 @@ void launch_inv(const LastArgs<R> &a, const Cfg &c, cudaStream_t s, int B = 1) {
   MUSG_CHECK_LAUNCH();
 }
 
+// register-resident passes (spectral_reg.cuh): lanes per pencil of a length
+int reg_lanes(int m) { return m == 16 || m == 32 ? 4 : m == 256 ? 16 : 8; }
+int RegLanesR1(int m) { return m == 16 ? 4 : (m == 32 || m == 64) ? 8 : 16; }
+bool reg_axis(const AxisPlan &p) { return !p.blu && p.m == p.n && reg_fft_length(p.n); }
+
+// tile of T pencils from the tuned shared-memory target, at most tmax, balanced over
+// the inner extent
+long reg_tile(long target, long per_pencil, long tmax, long long inner) {
+  long T = std::max(1L, std::min(tmax, target / per_pencil));
+  T = std::min<long>(T, (long)optin_smem() / per_pencil);
+  T = std::max(1L, std::min<long>(T, inner));
+  const long nt = (long)((inner + T - 1) / T);
+  return (long)((inner + nt - 1) / nt);
+}
+
+template <typename R, bool INV>
+void launch_axis_reg(int m, const AxisArgs<R> &a, dim3 grid, dim3 block, size_t smem, cudaStream_t s) {
+#define MUSG_AXR(M)                   \
+  case M: {                           \
+    auto k = k_axis_reg<R, M, INV>;   \
+    allow_smem(k);                    \
+    k<<<grid, block, smem, s>>>(a);   \
+    break;                            \
+  }
+  switch (m) {
+    MUSG_AXR(16) MUSG_AXR(32) MUSG_AXR(64) MUSG_AXR(128) MUSG_AXR(256)
+    default: throw Error(MUSG_ERR_ARGUMENT, "no register FFT of this length");
+  }
+#undef MUSG_AXR
+  MUSG_CHECK_LAUNCH();
+}
+
+template <typename R, int MODE, int D>
+void launch_green_reg(int m, const GreenArgs<R> &a, dim3 grid, dim3 block, size_t smem, cudaStream_t s) {
+#define MUSG_GRR(M)                          \
+  case M: {                                  \
+    auto k = k_green_reg<R, M, MODE, D>;     \
+    allow_smem(k);                           \
+    k<<<grid, block, smem, s>>>(a);          \
+    break;                                   \
+  }
+  switch (m) {
+    MUSG_GRR(16) MUSG_GRR(32) MUSG_GRR(64) MUSG_GRR(128) MUSG_GRR(256)
+    default: throw Error(MUSG_ERR_ARGUMENT, "no register FFT of this length");
+  }
+#undef MUSG_GRR
+  MUSG_CHECK_LAUNCH();
+}
+
+// last-axis register kernels (FP32 CG passes): rows per block G = 2 G2 with the
+// block (Y lanes, ncomp G2 pencils) a whole number of warps and at most 512 threads;
+// G = 0 when the axis or the shape does not allow them
+template <typename R> int last_reg_rows(const Spectral &sp) {
+  if (sizeof(R) != 4) return 0;
+  const AxisPlan &ap = sp.ax[sp.g.dim - 1];
+  if (!reg_axis(ap)) return 0;
+  const int m = ap.m, Y = reg_lanes(m), nc = sp.ncomp;
+  const long ps = (long)(m + m / RegLanesR1(m));
+  const long per_g2 = (long)nc * ps * (long)sizeof(typename V2<R>::T);
+  long g2 = std::max(1L, sp.tune_bytes[prec_index<R>()][0] / per_g2);
+  g2 = std::min<long>(g2, (sp.g.nrows + 1) / 2);
+  for (; g2 >= 1; --g2) {
+    const long th = (long)Y * nc * g2;
+    if (th <= 512 && th % 32 == 0 && g2 * per_g2 <= optin_smem()) return (int)(2 * g2);
+  }
+  return 0;
+}
+
+template <int D, int TK>
+void launch_fwd_reg(int m, const LastArgs<float> &a, dim3 grid, dim3 block, size_t smem, cudaStream_t s) {
+#define MUSG_LFR(M)                           \
+  case M: {                                   \
+    auto k = k_last_fwd_reg<M, D, TK>;        \
+    allow_smem(k);                            \
+    k<<<grid, block, smem, s>>>(a);           \
+    break;                                    \
+  }
+  switch (m) {
+    MUSG_LFR(16) MUSG_LFR(32) MUSG_LFR(64) MUSG_LFR(128) MUSG_LFR(256)
+    default: throw Error(MUSG_ERR_ARGUMENT, "no register FFT of this length");
+  }
+#undef MUSG_LFR
+  MUSG_CHECK_LAUNCH();
+}
+
+template <int D>
+void launch_inv_reg(int m, const LastArgs<float> &a, dim3 grid, dim3 block, size_t smem, cudaStream_t s) {
+#define MUSG_LIR(M)                           \
+  case M: {                                   \
+    auto k = k_last_inv_reg<M, D>;            \
+    allow_smem(k);                            \
+    k<<<grid, block, smem, s>>>(a);           \
+    break;                                    \
+  }
+  switch (m) {
+    MUSG_LIR(16) MUSG_LIR(32) MUSG_LIR(64) MUSG_LIR(128) MUSG_LIR(256)
+    default: throw Error(MUSG_ERR_ARGUMENT, "no register FFT of this length");
+  }
+#undef MUSG_LIR
+  MUSG_CHECK_LAUNCH();
+}
+
+// the two CG last-axis passes through the register kernels; returns the number of
+// partial sums (blocks)
+template <typename R>
+int last_cg_reg(Spectral &sp, int tkind, LastArgs<R> a, int G, bool inv, cudaStream_t s, int B) {
+  if constexpr (sizeof(R) != 4) {
+    throw Error(MUSG_ERR_RUNTIME, "register last-axis passes are FP32 only");
+  } else {
+    const int m = sp.ax[sp.g.dim - 1].m, Y = reg_lanes(m);
+    const int nc = sp.ncomp, G2 = G / 2;
+    const int blocks = (int)((sp.g.nrows + G - 1) / G);
+    const long ps = m + m / RegLanesR1(m);
+    a.G = G;
+    const dim3 grid(blocks, B), block(Y, nc * G2);
+    const size_t smem = (size_t)nc * G2 * ps * sizeof(float2);
+    if (!inv) {
+#define MUSG_FR(DD, TT) \
+  if (sp.g.dim == DD && tkind == TT) { launch_fwd_reg<DD, TT>(m, a, grid, block, smem, s); return blocks; }
+      MUSG_FR(2, TK_SMALL) MUSG_FR(2, TK_FINITE) MUSG_FR(2, TK_KPRIME) MUSG_FR(2, TK_MIXED) MUSG_FR(2, TK_FISO)
+      MUSG_FR(3, TK_SMALL) MUSG_FR(3, TK_FINITE) MUSG_FR(3, TK_KPRIME) MUSG_FR(3, TK_MIXED) MUSG_FR(3, TK_FISO)
+#undef MUSG_FR
+      throw Error(MUSG_ERR_ARGUMENT, "unsupported tangent kind");
+    }
+    if (sp.g.dim == 2) launch_inv_reg<2>(m, a, grid, block, smem, s);
+    else launch_inv_reg<3>(m, a, grid, block, smem, s);
+    return blocks;
+  }
+}
+
 template <typename R>
 void run_axis(Spectral &sp, bool inv, const CGState *st, cudaStream_t s, const ProblemPtrs<R> *batch = nullptr,
               int B = 1) {
   // 3-D only: pencils along axis 1 of [c][k0][k1][k2h]
   const long long inner = sp.g.nh;
   const long long nbatch = (long long)sp.ncomp * sp.g.n[0];
+  if (reg_axis(sp.ax[1])) {
+    using T = typename V2<R>::T;
+    const int m = sp.ax[1].m, Y = reg_lanes(m);
+    const long Tt = reg_tile(sp.tune_bytes[prec_index<R>()][1], (long)m * sizeof(T), std::min(32, 512 / Y), inner);
+    AxisArgs<R> a{};
+    a.ap = sp.ax[1].device<R>();
+    a.nax = m;
+    a.T = (int)Tt;
+    a.ntiles = (int)((inner + Tt - 1) / Tt);
+    a.se = sp.g.nh;
+    a.inner = inner;
+    a.sb = (long long)sp.g.n[1] * sp.g.nh;
+    a.spec = spec_of<R>(sp);
+    a.st = st;
+    a.batch = batch;
+    const dim3 grid((unsigned)(a.ntiles * nbatch), 1, B), block((unsigned)Tt, Y, 1);
+    const size_t smem = (size_t)Tt * m * sizeof(T);
+    if (inv) launch_axis_reg<R, true>(m, a, grid, block, smem, s);
+    else launch_axis_reg<R, false>(m, a, grid, block, smem, s);
+    return;
+  }
   const Cfg c = axis_cfg<R>(sp, 1, inner, nbatch);
   AxisArgs<R> a{};
   a.ap = sp.ax[1].device<R>();
@@ -209,6 +364,23 @@ void run_green(Spectral &sp, int mode, const CGState *st, cudaStream_t s, const 
   a.norm = R(1.0 / (double)sp.g.npx);
   a.st = st;
   a.batch = batch;
+  if (reg_axis(sp.ax[0]) && (mode == GM_SMALL || mode == GM_FINITE)) {
+    using T = typename V2<R>::T;
+    const int m = sp.ax[0].m, Y = reg_lanes(m);
+    const int nc = mode == GM_FINITE ? dim : dim * dim;
+    const int tmax = std::min(32, 512 / (Y * nc));
+    if (tmax >= 1) {
+      const long Tt = reg_tile(sp.tune_bytes[prec_index<R>()][2], (long)nc * m * sizeof(T), tmax, Rr);
+      a.T = (int)Tt;
+      const dim3 grid((unsigned)((Rr + Tt - 1) / Tt), mode == GM_FINITE ? dim : 1, B), block((unsigned)Tt, Y, nc);
+      const size_t smem = (size_t)nc * Tt * m * sizeof(T);
+      if (mode == GM_FINITE && dim == 2) launch_green_reg<R, GM_FINITE, 2>(m, a, grid, block, smem, s);
+      else if (mode == GM_FINITE) launch_green_reg<R, GM_FINITE, 3>(m, a, grid, block, smem, s);
+      else if (dim == 2) launch_green_reg<R, GM_SMALL, 2>(m, a, grid, block, smem, s);
+      else launch_green_reg<R, GM_SMALL, 3>(m, a, grid, block, smem, s);
+      return;
+    }
+  }
 #define MUSG_GREEN(MODE, DD)                                     \
   {                                                              \
     auto k = k_green<R, MODE, DD>;                               \
@@ -288,8 +460,10 @@ int cg_operator(Spectral &sp, int tkind, const TangentData<R> &td, const CGState
   auto mark = [&]() {
     if (ev) MUSG_CUDA(cudaEventRecord(ev[k++], s));
   };
+  const int greg = last_reg_rows<R>(sp);
   mark();
-  dispatch_fwd<R, PRO_CG>(sp.g.dim, tkind, a, c, s);
+  if (greg) last_cg_reg<R>(sp, tkind, a, greg, false, s, 1);
+  else dispatch_fwd<R, PRO_CG>(sp.g.dim, tkind, a, c, s);
   mark();
   if (sp.g.dim == 3) {
     run_axis<R>(sp, false, st, s);
@@ -300,6 +474,11 @@ int cg_operator(Spectral &sp, int tkind, const TangentData<R> &td, const CGState
   if (sp.g.dim == 3) {
     run_axis<R>(sp, true, st, s);
     mark();
+  }
+  if (greg) {
+    const int nb = last_cg_reg<R>(sp, tkind, a, greg, true, s, 1);
+    mark();
+    return nb;
   }
   if (sp.g.dim == 2) launch_inv<R, EPI_CG, 2>(a, c, s);
   else launch_inv<R, EPI_CG, 3>(a, c, s);
@@ -317,10 +496,13 @@ int cg_operator_batch(Spectral &sp, int tkind, const ProblemPtrs<R> *tab, int B,
   const Cfg c = last_cfg<R>(sp);
   LastArgs<R> a = last_args<R>(sp, c);
   a.batch = tab;
-  dispatch_fwd<R, PRO_CG>(sp.g.dim, tkind, a, c, s, B);
+  const int greg = last_reg_rows<R>(sp);
+  if (greg) last_cg_reg<R>(sp, tkind, a, greg, false, s, B);
+  else dispatch_fwd<R, PRO_CG>(sp.g.dim, tkind, a, c, s, B);
   if (sp.g.dim == 3) run_axis<R>(sp, false, nullptr, s, tab, B);
   run_green<R>(sp, gm, nullptr, s, tab, B);
   if (sp.g.dim == 3) run_axis<R>(sp, true, nullptr, s, tab, B);
+  if (greg) return last_cg_reg<R>(sp, tkind, a, greg, true, s, B);
   if (sp.g.dim == 2) launch_inv<R, EPI_CG, 2>(a, c, s, B);
   else launch_inv<R, EPI_CG, 3>(a, c, s, B);
   return c.blocks;
@@ -363,8 +545,11 @@ template <typename R> void spectral_autotune(Spectral &sp, cudaStream_t s, int e
       float best = 1e30f;
       int bt = sp.tune_threads[pi][pass];
       long bb = sp.tune_bytes[pi][pass];
+      // the register-resident passes take their block shape from the tile alone
+      const bool reg = (pass == 1 && reg_axis(sp.ax[1])) || (pass == 2 && reg_axis(sp.ax[0]) && gm != GM_FWD);
       for (int th : threads)
         for (long by : bytes) {
+          if (reg && th != threads[0]) continue;
           sp.tune_threads[pi][pass] = th;
           sp.tune_bytes[pi][pass] = by;
           float tot = 0;
