@@ -149,7 +149,6 @@ def algorithmic_bytes(name, npx, nk, d2, s, tm):
         'axis1_inv': 2 * spec,
         'last_axis_inv_dot': spec + 2 * u,                 # spectrum in; p in; Ap out
         'cg_update': 6 * u,                                # x, p, r, Ap in; x, r out
-        'cg_alpha': 0, 'cg_beta': 0,
     }.get(name, 0)
 
 
@@ -282,7 +281,7 @@ def main():
     peak, peak_kind = measured_peaks()
     d2 = 9
     nk = (npx // w['res'][-1]) * (w['res'][-1] // 2 + 1)
-    tm = 4 * (9 + 9 + 2)  # F, S (FP32) and lambda, mu per pixel
+    tm = 4 * (9 + 2)  # F - I and lambda, mu per pixel (FP32); the operator rebuilds S from F
     kern = {}
     for name, ms in prof.items():
         b = algorithmic_bytes(name, npx, nk, d2, 4, tm)

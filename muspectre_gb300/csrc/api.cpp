@@ -489,23 +489,19 @@ struct musg_solver {
     double *part = c.partial.as<double>();
     const TangentData<R> td = c.tangent<R>();
     const int nop = cg_operator<R>(c.sp, c.tk<R>(), td, d, r.as<R>(), p.as<R>(), Ap.as<R>(), part, s, ev);
+    (void)nop;  // the last pass finishes alpha over its own partial sums
     int k = c.dim == 3 ? 5 : 3;
-    cg_finalize_alpha(d, part, nop, s);
-    if (ev) MUSG_CUDA(cudaEventRecord(ev[++k], s));
-    cg_update<R>(d, x.as<R>(), r.as<R>(), p.as<R>(), Ap.as<R>(), n, part, s);
-    if (ev) MUSG_CUDA(cudaEventRecord(ev[++k], s));
-    cg_finalize_beta(d, part, update_blocks(n), s);
+    cg_update<R>(d, x.as<R>(), r.as<R>(), p.as<R>(), Ap.as<R>(), n, part, s);  // and beta
     if (ev) MUSG_CUDA(cudaEventRecord(ev[++k], s));
     return k;  // number of kernels
   }
 
   static const char *kernel_name(int dim, int k) {
     static const char *n3[] = {"last_axis_fwd_tangent", "axis1_fwd", "green_axis0", "axis1_inv", "last_axis_inv_dot",
-                               "cg_alpha", "cg_update", "cg_beta"};
-    static const char *n2[] = {"last_axis_fwd_tangent", "green_axis0", "last_axis_inv_dot", "cg_alpha", "cg_update",
-                               "cg_beta"};
-    if (dim == 3) return (k >= 0 && k < 8) ? n3[k] : "";
-    return (k >= 0 && k < 6) ? n2[k] : "";
+                               "cg_update"};
+    static const char *n2[] = {"last_axis_fwd_tangent", "green_axis0", "last_axis_inv_dot", "cg_update"};
+    if (dim == 3) return (k >= 0 && k < 6) ? n3[k] : "";
+    return (k >= 0 && k < 4) ? n2[k] : "";
   }
 
   // mean per-kernel durations (ms) over `iters` eagerly launched iterations started
@@ -517,7 +513,7 @@ struct musg_solver {
     const long long n = c.nb_dof();
     double *part = c.partial.as<double>();
     cg_init<R>(st.as<CGState>(), c.rhs.as<double>(), r.as<R>(), x.as<R>(), n, 0.0, iters, part, part + 4096, s);
-    const int nk = c.dim == 3 ? 8 : 6;
+    const int nk = c.dim == 3 ? 6 : 4;
     std::vector<cudaEvent_t> ev(nk + 1);
     for (auto &e : ev) MUSG_CUDA(cudaEventCreate(&e));
     std::vector<double> acc(nk, 0.0);
@@ -667,10 +663,8 @@ struct musg_batch {
   template <typename R> void iteration(cudaStream_t s) {
     musg_cell &c0 = *cells[0];
     const long long n = c0.nb_dof();
-    const int nop = cg_operator_batch<R>(c0.sp, c0.tk<R>(), (const ProblemPtrs<R> *)tab_p.p, B(), s);
-    cg_finalize_alpha_batch<R>(tab_v.as<BatchVec<R>>(), nop, B(), s);
-    cg_update_batch<R>(tab_v.as<BatchVec<R>>(), n, B(), s);
-    cg_finalize_beta_batch<R>(tab_v.as<BatchVec<R>>(), update_blocks(n), B(), s);
+    cg_operator_batch<R>(c0.sp, c0.tk<R>(), (const ProblemPtrs<R> *)tab_p.p, B(), s);  // and alpha
+    cg_update_batch<R>(tab_v.as<BatchVec<R>>(), n, B(), s);                              // and beta
   }
 
   template <typename R> void build_graph() {

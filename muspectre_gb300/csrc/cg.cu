@@ -4,8 +4,8 @@
 // beta, the iteration count and an `active` flag).  Every kernel of an iteration
 // returns at once when `active` is 0, so a CUDA graph holding several iterations
 // can be replayed past convergence without changing the result.  Dot products are
-// reduced in two deterministic stages (fixed block partition, then one block in a
-// fixed order), so a rerun gives bit-identical scalars.  FP32 vectors are
+// reduced in two deterministic stages (fixed block partition, then the last block to
+// finish sums the partials in a fixed order), so a rerun gives bit-identical scalars.  FP32 vectors are
 // accumulated with Neumaier-compensated FP32 sums per thread and FP64 across
 // threads and blocks.
 #include <algorithm>
@@ -64,6 +64,7 @@ __global__ void k_cg_init_scalars(CGState *st, const double *partial, const doub
     st->alpha = st->beta = st->pAp = 0.0;
     st->iter = 0;
     st->maxiter = maxiter;
+    st->ticket = 0;
     // solver_cg.cc:76-77: i < maxiter && (rdr > tol2 || i == 0)
     st->active = maxiter > 0 ? 1 : 0;
   }
@@ -126,11 +127,12 @@ __device__ __forceinline__ double cg_update_body(R alpha, R *__restrict__ x, R *
 }
 
 template <typename R>
-__global__ void k_cg_update(const CGState *__restrict__ st, R *__restrict__ x, R *__restrict__ r,
+__global__ void k_cg_update(CGState *__restrict__ st, R *__restrict__ x, R *__restrict__ r,
                             const R *__restrict__ p, const R *__restrict__ Ap, long long n, double *partial) {
   if (!st->active) return;
   const double bs = cg_update_body<R>(R(st->alpha), x, r, p, Ap, n);
   if (threadIdx.x == 0) partial[blockIdx.x] = bs;
+  if (cg_last_block(st)) cg_beta_step(st, partial, gridDim.x);
 }
 
 int update_blocks(long long n) {
@@ -146,43 +148,10 @@ int update_blocks(long long n) {
 inline bool aligned16(const void *q) { return ((uintptr_t)q & 15u) == 0; }
 
 template <typename R>
-void cg_update(const CGState *st, R *x, R *r, const R *p, const R *Ap, long long n, double *partial, cudaStream_t s) {
+void cg_update(CGState *st, R *x, R *r, const R *p, const R *Ap, long long n, double *partial, cudaStream_t s) {
   if (!(aligned16(x) && aligned16(r) && aligned16(p) && aligned16(Ap)))
     throw Error(MUSG_ERR_ARGUMENT, "CG vectors must be 16-byte aligned");
   k_cg_update<R><<<update_blocks(n), kRedThreads, 0, s>>>(st, x, r, p, Ap, n, partial);
-  MUSG_CHECK_LAUNCH();
-}
-
-__global__ void k_cg_alpha(CGState *st, const double *partial, int nparts) {
-  if (!st->active) return;
-  const double pAp = sum_partials(partial, nparts);
-  if (threadIdx.x == 0) {
-    st->pAp = pAp;
-    st->alpha = st->rdr / pAp;  // solver_cg.cc:81
-  }
-}
-
-__global__ void k_cg_beta(CGState *st, const double *partial, int nparts) {
-  if (!st->active) return;
-  const double new_rdr = sum_partials(partial, nparts);
-  if (threadIdx.x == 0) {
-    st->beta = new_rdr / st->rdr;  // solver_cg.cc:86-88
-    st->rdr = new_rdr;
-    st->iter += 1;
-    st->counter += 1;
-    // loop condition for the next iteration (i >= 1 from here on); a non-finite
-    // residual fails the comparison and ends the loop, as in the reference
-    if (!(st->iter < st->maxiter && st->rdr > st->tol2)) st->active = 0;
-  }
-}
-
-void cg_finalize_alpha(CGState *st, const double *partial, int nparts, cudaStream_t s) {
-  k_cg_alpha<<<1, 1024, 0, s>>>(st, partial, nparts);
-  MUSG_CHECK_LAUNCH();
-}
-
-void cg_finalize_beta(CGState *st, const double *partial, int nparts, cudaStream_t s) {
-  k_cg_beta<<<1, 1024, 0, s>>>(st, partial, nparts);
   MUSG_CHECK_LAUNCH();
 }
 
@@ -193,29 +162,7 @@ __global__ void k_cg_update_b(const BatchVec<R> *tab, long long n) {
   if (!q.st->active) return;
   const double bs = cg_update_body<R>(R(q.st->alpha), q.x, q.r, q.p, q.Ap, n);
   if (threadIdx.x == 0) q.partial[blockIdx.x] = bs;
-}
-
-template <typename R> __global__ void k_cg_alpha_b(const BatchVec<R> *tab, int nparts) {
-  CGState *st = tab[blockIdx.x].st;
-  if (!st->active) return;
-  const double pAp = sum_partials(tab[blockIdx.x].partial, nparts);
-  if (threadIdx.x == 0) {
-    st->pAp = pAp;
-    st->alpha = st->rdr / pAp;
-  }
-}
-
-template <typename R> __global__ void k_cg_beta_b(const BatchVec<R> *tab, int nparts) {
-  CGState *st = tab[blockIdx.x].st;
-  if (!st->active) return;
-  const double new_rdr = sum_partials(tab[blockIdx.x].partial, nparts);
-  if (threadIdx.x == 0) {
-    st->beta = new_rdr / st->rdr;
-    st->rdr = new_rdr;
-    st->iter += 1;
-    st->counter += 1;
-    if (!(st->iter < st->maxiter && st->rdr > st->tol2)) st->active = 0;
-  }
+  if (cg_last_block(q.st)) cg_beta_step(q.st, q.partial, gridDim.x);
 }
 
 template <typename R> void cg_update_batch(const BatchVec<R> *tab, long long n, int B, cudaStream_t s) {
@@ -223,22 +170,8 @@ template <typename R> void cg_update_batch(const BatchVec<R> *tab, long long n, 
   MUSG_CHECK_LAUNCH();
 }
 
-template <typename R> void cg_finalize_alpha_batch(const BatchVec<R> *tab, int nparts, int B, cudaStream_t s) {
-  k_cg_alpha_b<R><<<B, 1024, 0, s>>>(tab, nparts);
-  MUSG_CHECK_LAUNCH();
-}
-
-template <typename R> void cg_finalize_beta_batch(const BatchVec<R> *tab, int nparts, int B, cudaStream_t s) {
-  k_cg_beta_b<R><<<B, 1024, 0, s>>>(tab, nparts);
-  MUSG_CHECK_LAUNCH();
-}
-
 template void cg_update_batch<double>(const BatchVec<double> *, long long, int, cudaStream_t);
 template void cg_update_batch<float>(const BatchVec<float> *, long long, int, cudaStream_t);
-template void cg_finalize_alpha_batch<double>(const BatchVec<double> *, int, int, cudaStream_t);
-template void cg_finalize_alpha_batch<float>(const BatchVec<float> *, int, int, cudaStream_t);
-template void cg_finalize_beta_batch<double>(const BatchVec<double> *, int, int, cudaStream_t);
-template void cg_finalize_beta_batch<float>(const BatchVec<float> *, int, int, cudaStream_t);
 
 // ------------------------------------------------------------------ dots
 template <typename Ra, typename Rb>
@@ -318,9 +251,9 @@ template void cg_init<double>(CGState *, const double *, double *, double *, lon
                               double *, cudaStream_t);
 template void cg_init<float>(CGState *, const double *, float *, float *, long long, double, int, double *, double *,
                              cudaStream_t);
-template void cg_update<double>(const CGState *, double *, double *, const double *, const double *, long long,
+template void cg_update<double>(CGState *, double *, double *, const double *, const double *, long long,
                                 double *, cudaStream_t);
-template void cg_update<float>(const CGState *, float *, float *, const float *, const float *, long long, double *,
+template void cg_update<float>(CGState *, float *, float *, const float *, const float *, long long, double *,
                                cudaStream_t);
 template void dot_device<double, double>(const double *, const double *, long long, double *, double *, cudaStream_t);
 template void dot_device<float, float>(const float *, const float *, long long, double *, double *, cudaStream_t);

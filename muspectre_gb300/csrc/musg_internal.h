@@ -111,7 +111,7 @@ struct CGState {
   int iter;          // iterations of this solve
   int maxiter;
   int active;        // 1 while the loop runs
-  int pad;
+  int ticket;        // blocks of the running kernel that have written their partial sum
   unsigned long long counter;  // cumulative iterations (SolverBase::counter)
 };
 
@@ -156,8 +156,9 @@ template <typename R>
 void spectral_project(Spectral &sp, const R *in, R *out, R in_scale, cudaStream_t s);
 
 // CG operator application, fused: p = -r + beta p (or p = -r on the first
-// iteration), Ap = G(K:p), partial[b] = block sums of p.Ap.  Returns the number of
-// partial sums written (blocks of the last pass).
+// iteration), Ap = G(K:p), partial[b] = block sums of p.Ap, and alpha = r.r / p.Ap
+// in the state (by the last block of the last pass).  Returns the number of partial
+// sums written (blocks of the last pass).
 // ev (optional): an event is recorded before the first and after every kernel
 template <typename R>
 int cg_operator(Spectral &sp, int tkind, const TangentData<R> &td, const CGState *st,
@@ -195,10 +196,8 @@ template <typename R>
 void cg_init(CGState *st, const double *rhs, R *r, R *x, long long n, double tol,
              int maxiter, double *partial, double *partial2, cudaStream_t s);
 template <typename R>
-void cg_update(const CGState *st, R *x, R *r, const R *p, const R *Ap, long long n,
+void cg_update(CGState *st, R *x, R *r, const R *p, const R *Ap, long long n,
                double *partial, cudaStream_t s);
-void cg_finalize_alpha(CGState *st, const double *partial, int nparts, cudaStream_t s);
-void cg_finalize_beta(CGState *st, const double *partial, int nparts, cudaStream_t s);
 // batched variants: per-problem pointer tables (device arrays of B entries)
 template <typename R> struct BatchVec {
   CGState *st;
@@ -210,10 +209,6 @@ template <typename R> struct BatchVec {
 };
 template <typename R>
 void cg_update_batch(const BatchVec<R> *tab, long long n, int B, cudaStream_t s);
-template <typename R>
-void cg_finalize_alpha_batch(const BatchVec<R> *tab, int nparts, int B, cudaStream_t s);
-template <typename R>
-void cg_finalize_beta_batch(const BatchVec<R> *tab, int nparts, int B, cudaStream_t s);
 // FP64 dot of a with b over n entries into *out_device (deterministic)
 template <typename Ra, typename Rb>
 void dot_device(const Ra *a, const Rb *b, long long n, double *partial, double *out,

@@ -68,6 +68,57 @@ __device__ __forceinline__ double block_sum(double v) {
   return v;
 }
 
+// ------------------------------------------------------------ CG scalar steps
+// The kernel that produces a dot product's partial sums also finishes it: every block
+// writes partial[blockIdx.x], and the block that finishes last (counted with the
+// state's ticket) sums all gridDim.x partials in a fixed order and updates the state.
+// Deterministic like a separate reduction kernel, without its launch.
+__device__ __forceinline__ int lin_tid() { return threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z); }
+__device__ __forceinline__ int lin_nth() { return blockDim.x * blockDim.y * blockDim.z; }
+
+// call by the whole block after thread 0 wrote this block's partial sum
+__device__ __forceinline__ bool cg_last_block(CGState *st) {
+  __shared__ int last;
+  __syncthreads();
+  if (lin_tid() == 0) {
+    __threadfence();
+    last = atomicAdd(&st->ticket, 1) == (int)gridDim.x - 1;
+  }
+  __syncthreads();
+  return last != 0;
+}
+
+__device__ __forceinline__ double sum_partials_fresh(const double *partial, int n) {
+  double v = 0.0;
+  for (int i = lin_tid(); i < n; i += lin_nth()) v += __ldcg(partial + i);
+  return block_sum(v);
+}
+
+// alpha = r.r / p.Ap (solver_cg.cc:81)
+__device__ __forceinline__ void cg_alpha_step(CGState *st, const double *partial, int n) {
+  const double pAp = sum_partials_fresh(partial, n);
+  if (lin_tid() == 0) {
+    st->pAp = pAp;
+    st->alpha = st->rdr / pAp;
+    st->ticket = 0;
+  }
+}
+
+// beta = new r.r / old r.r (solver_cg.cc:86-88) and the loop condition of the next
+// iteration; a non-finite residual fails the comparison and ends the loop, as in the
+// reference
+__device__ __forceinline__ void cg_beta_step(CGState *st, const double *partial, int n) {
+  const double nr = sum_partials_fresh(partial, n);
+  if (lin_tid() == 0) {
+    st->beta = nr / st->rdr;
+    st->rdr = nr;
+    st->iter += 1;
+    st->counter += 1;
+    if (!(st->iter < st->maxiter && st->rdr > st->tol2)) st->active = 0;
+    st->ticket = 0;
+  }
+}
+
 // ------------------------------------------------------------ tangents
 // small strain, isotropic: lam tr(e) I + mu (e + e^T)
 template <int D, typename R>
@@ -439,6 +490,8 @@ __global__ void __launch_bounds__(kPassThreads) k_last_inv(const LastArgs<R> a0)
     }
     const double bs = block_sum(acc.value());
     if (threadIdx.x == 0) a.partial[blockIdx.x] = bs;
+    CGState *st = const_cast<CGState *>(a.st);
+    if (cg_last_block(st)) cg_alpha_step(st, a.partial, gridDim.x);
   }
 }
 

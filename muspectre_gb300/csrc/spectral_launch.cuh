@@ -207,7 +207,7 @@ void launch_green_reg(int m, const GreenArgs<R> &a, dim3 grid, dim3 block, size_
 }
 
 // last-axis register kernels (FP32 CG passes): rows per block G = 2 G2 with the
-// block (Y lanes, ncomp G2 pencils) a whole number of warps and at most 512 threads;
+// block (Y lanes, ncomp G2 pencils) a whole number of warps and at most 384 threads;
 // G = 0 when the axis or the shape does not allow them
 template <typename R> int last_reg_rows(const Spectral &sp) {
   if (sizeof(R) != 4) return 0;
@@ -220,7 +220,7 @@ template <typename R> int last_reg_rows(const Spectral &sp) {
   g2 = std::min<long>(g2, (sp.g.nrows + 1) / 2);
   for (; g2 >= 1; --g2) {
     const long th = (long)Y * nc * g2;
-    if (th <= 512 && th % 32 == 0 && g2 * per_g2 <= optin_smem()) return (int)(2 * g2);
+    if (th <= 384 && th % 32 == 0 && g2 * per_g2 <= optin_smem()) return (int)(2 * g2);  // k_last_inv_reg bound
   }
   return 0;
 }
@@ -368,7 +368,7 @@ void run_green(Spectral &sp, int mode, const CGState *st, cudaStream_t s, const 
     using T = typename V2<R>::T;
     const int m = sp.ax[0].m, Y = reg_lanes(m);
     const int nc = mode == GM_FINITE ? dim : dim * dim;
-    const int tmax = std::min(32, 512 / (Y * nc));
+    const int tmax = std::min(32, 384 / (Y * nc));  // k_green_reg: at most 384 threads
     if (tmax >= 1) {
       const long Tt = reg_tile(sp.tune_bytes[prec_index<R>()][2], (long)nc * m * sizeof(T), tmax, Rr);
       a.T = (int)Tt;

@@ -125,7 +125,7 @@ __global__ void __launch_bounds__(512) k_axis_reg(const AxisArgs<R> a0) {
 // gridDim.y = 1.  blockIdx.z = problem of a batched launch.  Shared memory:
 // slot-major [slot][z][t], NC * T pencils of M entries.
 template <typename R, int M, int MODE, int D>
-__global__ void __launch_bounds__(512) k_green_reg(const GreenArgs<R> a0) {
+__global__ void __launch_bounds__(384, 2) k_green_reg(const GreenArgs<R> a0) {
   using T = typename V2<R>::T;
   using F = RegFft<M>;
   static_assert(MODE == GM_SMALL || MODE == GM_FINITE, "projection modes only");
@@ -331,7 +331,7 @@ __global__ void __launch_bounds__(512) k_last_fwd_reg(const LastArgs<float> a0) 
 // of p.Ap over the block's rows.  The p entries of a lane's outputs are loaded before
 // the transform so that they are in flight with the spectrum.  FP32 only.
 template <int M, int D>
-__global__ void __launch_bounds__(512) k_last_inv_reg(const LastArgs<float> a0) {
+__global__ void __launch_bounds__(384, 2) k_last_inv_reg(const LastArgs<float> a0) {
   using R = float;
   using T = float2;
   using F = RegFft<M>;
@@ -404,6 +404,8 @@ __global__ void __launch_bounds__(512) k_last_inv_reg(const LastArgs<float> a0) 
   }
   const double bs = block_sum(acc.value());
   if (y == 0 && q == 0) a.partial[blockIdx.x] = bs;
+  CGState *st = const_cast<CGState *>(a.st);
+  if (cg_last_block(st)) cg_alpha_step(st, a.partial, gridDim.x);
 }
 
 }  // namespace musg
