@@ -131,6 +131,11 @@ int musg_cell_evaluate_stress_tangent(musg_cell *cell, double *stress_out,
                                       double *tangent_out);
 /* Cell::apply_projection (cell_base.cc:202-208): in place on a host vector */
 int musg_cell_apply_projection(musg_cell *cell, double *vec);
+/* homogenised stress: the pixel mean of the cell's stress field (D*D doubles,
+ * column-major), the metric quantity; the reference forms it on the host from
+ * OptimizeResult::stress (the idiom of solvers.cc:197).  Reduced on the device in a
+ * fixed order, so it is identical for a cell however it was solved. */
+int musg_cell_homogenised_stress(musg_cell *cell, double *out);
 /* Cell::evaluate_projected_directional_stiffness (cell_base.cc:150-192) */
 int musg_cell_directional_stiffness(musg_cell *cell, const double *dF, double *dP);
 /* G(K:dF) through the kernels of one CG iteration (the operator SolverCG applies) in
@@ -182,6 +187,76 @@ int musg_batch_set_inner_tol(musg_batch *batch, double inner_tol);
 int musg_batch_newton_cg(musg_batch *batch, const double *load_steps, int nb_steps,
                          double newton_tol, double equil_tol, musg_result_info *infos,
                          double *stresses);
+
+/* ---------------------------------------------------------- serving
+ * A continuous-batching request server (no counterpart in the reference, which
+ * solves one cell per process).  Requests are admitted while their estimated device
+ * footprint (musg_request_bytes) fits the HBM budget next to the requests already
+ * running; waiting requests of the same shape (grid, formulation, material-law
+ * kind, number of load steps) are taken together and solved as one batch
+ * (musg_batch_*).  Each lane is a host thread with its own CUDA stream, so admitted
+ * work overlaps on the device; a request's fields and plastic state stay on the
+ * device for all its load steps and return to the budget when it completes.  Every
+ * request gets the same kernels in the same order alone or in a batch, so its result
+ * does not depend on what else runs. */
+typedef struct musg_server musg_server;
+
+/* one request; the server copies everything at submission */
+typedef struct musg_request {
+  int dim;                    /* 2 or 3                                              */
+  int resolutions[3];
+  double lengths[3];
+  int formulation;            /* MUSG_FINITE_STRAIN / MUSG_SMALL_STRAIN               */
+  int flags;                  /* MUSG_FLAG_*                                          */
+  int nb_materials;           /* <= 256                                               */
+  const int *laws;            /* nb_materials MUSG_LAW_*                              */
+  const double *params;       /* nb_materials x 5: the law's parameters (E, nu[, tau_y0, H, logm mode]) */
+  const unsigned char *phase; /* material index of every pixel (row-major)            */
+  const double *per_pixel;    /* LE3/LE4: (E, nu); LE2: D*D eigenstrain (column-major); NULL if unused */
+  int per_pixel_stride;       /* doubles per pixel in per_pixel                        */
+  int nb_steps;
+  const double *load_steps;   /* nb_steps D*D column-major macroscopic increments     */
+} musg_request;
+
+typedef struct musg_server_result {
+  long long id;
+  int success;                /* every load step converged                           */
+  int nb_steps_done;
+  unsigned nb_it;             /* Newton iterations of the last load step             */
+  unsigned nb_fev;            /* CG iterations of the last load step                 */
+  double stress[9];           /* homogenised stress after the last step (column-major) */
+  double latency_s;           /* completion - submission                             */
+  int batched_with;           /* requests of the batch it was solved in              */
+  char message[64];
+} musg_server_result;
+
+typedef struct musg_server_stats {
+  long long submitted, completed, batches;
+  unsigned long long budget, in_use, peak_in_use;
+} musg_server_stats;
+
+/* device bytes a request holds while it runs (fields, spectra, tangent data, CG
+ * vectors, state), for the precision it runs in */
+int musg_request_bytes(const musg_request *req, int precision, unsigned long long *bytes);
+/* lanes = 0 starts no thread and touches no GPU: musg_server_admit / _release then
+ * step the admission by hand (host-side checks of the policy) */
+int musg_server_create(unsigned long long hbm_budget, int lanes, int max_batch, int precision,
+                       double tol, unsigned maxiter, double newton_tol, musg_server **out);
+int musg_server_submit(musg_server *srv, const musg_request *req, long long *id);
+/* no more submissions; lanes finish the queue and exit */
+int musg_server_close(musg_server *srv);
+/* result of request id, waiting at most timeout_s seconds (MUSG_ERR_RUNTIME when it
+ * is not done by then); a result can be fetched once */
+int musg_server_wait(musg_server *srv, long long id, double timeout_s, musg_server_result *out);
+int musg_server_get_stats(musg_server *srv, musg_server_stats *out);
+/* closes the server and joins its lanes */
+int musg_server_destroy(musg_server *srv);
+/* the admission step of a lane: the oldest waiting request that fits the budget
+ * (or any request when nothing runs) and the waiting requests of its shape that fit
+ * too, at most cap; their ids, count and bytes (now counted as in use) */
+int musg_server_admit(musg_server *srv, long long *ids, int cap, int *count, unsigned long long *bytes);
+/* returns bytes of a finished group to the budget */
+int musg_server_release(musg_server *srv, unsigned long long bytes);
 
 /* ---------------------------------------------------------- instrumentation
  * (no counterpart in the reference, which has no device)

@@ -44,6 +44,25 @@ class ResultInfo(C.Structure):
                 ('message', C.c_char * 64)]
 
 
+class Request(C.Structure):
+    _fields_ = [('dim', C.c_int), ('resolutions', C.c_int * 3), ('lengths', C.c_double * 3),
+                ('formulation', C.c_int), ('flags', C.c_int), ('nb_materials', C.c_int),
+                ('laws', C.POINTER(C.c_int)), ('params', C.POINTER(C.c_double)),
+                ('phase', C.POINTER(C.c_ubyte)), ('per_pixel', C.POINTER(C.c_double)),
+                ('per_pixel_stride', C.c_int), ('nb_steps', C.c_int), ('load_steps', C.POINTER(C.c_double))]
+
+
+class ServerResult(C.Structure):
+    _fields_ = [('id', C.c_longlong), ('success', C.c_int), ('nb_steps_done', C.c_int), ('nb_it', C.c_uint),
+                ('nb_fev', C.c_uint), ('stress', C.c_double * 9), ('latency_s', C.c_double),
+                ('batched_with', C.c_int), ('message', C.c_char * 64)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [('submitted', C.c_longlong), ('completed', C.c_longlong), ('batches', C.c_longlong),
+                ('budget', C.c_ulonglong), ('in_use', C.c_ulonglong), ('peak_in_use', C.c_ulonglong)]
+
+
 _P = C.c_void_p
 _D = C.POINTER(C.c_double)
 _I = C.POINTER(C.c_int)
@@ -72,6 +91,7 @@ _SIGNATURES = {
     'musg_cell_directional_stiffness': (C.c_int, [_P, _D, _D]),
     'musg_cell_cg_operator': (C.c_int, [_P, C.c_int, _D, _D]),
     'musg_cell_save_history_variables': (C.c_int, [_P]),
+    'musg_cell_homogenised_stress': (C.c_int, [_P, _D]),
     'musg_solver_cg_create': (C.c_int, [_P, C.c_double, C.c_uint, C.c_int, C.c_int, C.POINTER(_P)]),
     'musg_solver_destroy': (C.c_int, [_P]),
     'musg_solver_set_inner_tol': (C.c_int, [_P, C.c_double]),
@@ -96,6 +116,16 @@ _SIGNATURES = {
     'musg_projection_destroy': (C.c_int, [_P]),
     'musg_projection_apply': (C.c_int, [_P, _D]),
     'musg_projection_get_operator': (C.c_int, [_P, _D, _LL, _LL]),
+    'musg_request_bytes': (C.c_int, [C.POINTER(Request), C.c_int, C.POINTER(C.c_ulonglong)]),
+    'musg_server_create': (C.c_int, [C.c_ulonglong, C.c_int, C.c_int, C.c_int, C.c_double, C.c_uint, C.c_double,
+                                     C.POINTER(_P)]),
+    'musg_server_submit': (C.c_int, [_P, C.POINTER(Request), _LL]),
+    'musg_server_close': (C.c_int, [_P]),
+    'musg_server_wait': (C.c_int, [_P, C.c_longlong, C.c_double, C.POINTER(ServerResult)]),
+    'musg_server_get_stats': (C.c_int, [_P, C.POINTER(ServerStats)]),
+    'musg_server_destroy': (C.c_int, [_P]),
+    'musg_server_admit': (C.c_int, [_P, _LL, C.c_int, _I, C.POINTER(C.c_ulonglong)]),
+    'musg_server_release': (C.c_int, [_P, C.c_ulonglong]),
     'musg_projection_apply_noalloc': (C.c_int, [C.c_int, _I, _D, C.c_int, C.c_int, _P, _P, _P]),
 }
 

@@ -41,6 +41,12 @@ void require(bool ok, int code, const std::string &msg) {
   if (!ok) throw Error(code, msg);
 }
 
+}  // namespace
+
+int musg::guarded(const std::function<void()> &f) { return guard(f); }
+
+namespace {
+
 // Hooke helpers (src/materials/materials_toolbox.hh:491-525)
 double lame_lambda(double E, double nu) { return E * nu / ((1 + nu) * (1 - 2 * nu)); }
 double lame_mu(double E, double nu) { return E / (2 * (1 + nu)); }
@@ -1172,6 +1178,18 @@ int musg_cell_get_stress(musg_cell *cell, double *out) {
   return guard([&] {
     require(cell && out, MUSG_ERR_ARGUMENT, "null argument");
     cell->download_field(cell->P.as<double>(), out);
+  });
+}
+
+int musg_cell_homogenised_stress(musg_cell *cell, double *out) {
+  return guard([&] {
+    require(cell && out, MUSG_ERR_ARGUMENT, "null argument");
+    musg_cell &c = *cell;
+    require(c.initialised, MUSG_ERR_RUNTIME, "the cell is not initialised");
+    double *d = c.scal.as<double>() + 40;
+    plane_means(c.P.as<double>(), c.D2, c.npx, c.partial.as<double>(), d, c.stream);
+    MUSG_CUDA(cudaMemcpyAsync(out, d, c.D2 * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+    MUSG_CUDA(cudaStreamSynchronize(c.stream));
   });
 }
 

@@ -235,6 +235,30 @@ void newton_update(double *F, const R *x, long long n, double *partial, double *
   MUSG_CHECK_LAUNCH();
 }
 
+// per-component means of a field [ncomp][npx]: deterministic block sums, then one
+// block per component in a fixed order
+__global__ void k_plane_sums(const double *__restrict__ f, long long npx, double *partial) {
+  const double *fc = f + (long long)blockIdx.y * npx;
+  double v = 0.0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < npx; i += (long long)gridDim.x * blockDim.x)
+    v += fc[i];
+  const double bs = block_sum(v);
+  if (threadIdx.x == 0) partial[blockIdx.y * gridDim.x + blockIdx.x] = bs;
+}
+
+__global__ void k_plane_finish(const double *partial, int nparts, double scale, double *out) {
+  const double v = sum_partials(partial + blockIdx.x * nparts, nparts);
+  if (threadIdx.x == 0) out[blockIdx.x] = v * scale;
+}
+
+void plane_means(const double *f, int ncomp, long long npx, double *partial, double *out, cudaStream_t s) {
+  const int nb = std::min(reduce_blocks(npx), 1024);
+  k_plane_sums<<<dim3(nb, ncomp), kRedThreads, 0, s>>>(f, npx, partial);
+  MUSG_CHECK_LAUNCH();
+  k_plane_finish<<<ncomp, 1024, 0, s>>>(partial, nb, 1.0 / (double)npx, out);
+  MUSG_CHECK_LAUNCH();
+}
+
 template <typename Rd, typename Rs>
 __global__ void k_convert(Rd *__restrict__ dst, const Rs *__restrict__ src, long long n, double scale) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)

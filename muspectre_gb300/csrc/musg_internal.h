@@ -6,6 +6,7 @@
 
 #include <atomic>
 #include <cstdint>
+#include <functional>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -18,6 +19,10 @@ struct Error : std::runtime_error {
   int code;
   Error(int c, const std::string &m) : std::runtime_error(m), code(c) {}
 };
+
+// Runs f, maps an exception to a status code and the calling thread's last-error
+// message (the C-ABI convention of every musg_* entry point)
+int guarded(const std::function<void()> &f);
 
 #define MUSG_CUDA(call)                                                              \
   do {                                                                               \
@@ -190,6 +195,9 @@ template <typename R> void spectral_autotune(Spectral &sp, cudaStream_t s, int e
 
 // ---------------------------------------------------------------- CG kernels (cg.cu)
 int reduce_blocks(long long n);
+// per-component means of a field [ncomp][npx] into out[ncomp] (device); partial
+// holds ncomp * 1024 doubles
+void plane_means(const double *f, int ncomp, long long npx, double *partial, double *out, cudaStream_t s);
 // blocks (= partial sums) of cg_update / cg_update_batch for n entries
 int update_blocks(long long n);
 template <typename R>

@@ -1,14 +1,13 @@
-"""Continuous-batching request server for homogenization solves.
+"""Continuous-batching request server: the Python face of musg_server_* (include/musg.h).
 
 Requests (one RVE each: grid, formulation, microstructure, load path) arrive over
-time.  ``Server`` admits a request when a lane is free and its estimated device
-footprint fits the HBM budget next to everything already admitted; requests of the
-same shape that are waiting together are taken as one batch
-(``batch.BatchSolver``: one launch per CG pass for all of them).  Each lane is a host
-thread whose cells run on their own CUDA streams, so admitted requests overlap on
-the device; the C library releases the GIL inside every call.  Fields and plastic
-state stay on the device for all load steps of a request; memory returns to the
-budget when the request completes.  Latency = completion - arrival.
+time.  The native server admits a request when a lane is free and its estimated
+device footprint fits the HBM budget next to everything already admitted; waiting
+requests of the same shape are taken together and solved as one batch (one launch
+per CG pass for all of them).  Each lane is a native host thread with its own CUDA
+stream, so admitted requests overlap on the device.  Fields and plastic state stay on
+the device for all load steps of a request; memory returns to the budget when the
+request completes.  Latency = completion - submission.
 
 Every request is computed by the same deterministic kernels whether it runs alone
 or in the mix (per-request reductions in a fixed order), which
@@ -16,18 +15,18 @@ or in the mix (per-request reductions in a fixed order), which
 """
 from __future__ import annotations
 
-import heapq
-import threading
+import ctypes as C
 import time
-from collections import deque
-from dataclasses import dataclass, field
+from dataclasses import dataclass
 from typing import Dict, List, Optional
 
 import numpy as np
 
-from . import batch as _batch
-from . import solvers as _solvers
-from .cell import Cell, Formulation
+from . import _lib as L
+from .cell import Formulation
+
+_LAWS = {'le1': L.LAW_LE1, 'le2': L.LAW_LE2, 'le3': L.LAW_LE3, 'le4': L.LAW_LE4, 'hep1': L.LAW_HEP1}
+_PREC = {'fp64': L.PRECISION_FP64, 'mixed': L.PRECISION_MIXED}
 
 
 @dataclass
@@ -61,67 +60,64 @@ class Result:
     batched_with: int = 1
 
 
+def _native(req):
+    """musg_request for req, and the arrays it points into (kept alive by the caller)."""
+    d = len(req.res)
+    npx = int(np.prod(req.res))
+    nm = len(req.materials)
+    laws = np.array([_LAWS[m[0]] for m in req.materials], dtype=np.int32)
+    params = np.zeros((nm, 5))
+    phase = np.ascontiguousarray(np.asarray(req.phase).reshape(-1), dtype=np.uint8)
+    per_pixel = None
+    for k, (law, prm) in enumerate(req.materials):
+        if law == 'le4' or law == 'le3':
+            if per_pixel is None:
+                per_pixel = np.zeros((npx, 2))
+            idx = np.flatnonzero(phase == k)
+            per_pixel[idx, 0] = np.asarray(prm[0], dtype=np.float64).reshape(-1)
+            per_pixel[idx, 1] = np.asarray(prm[1], dtype=np.float64).reshape(-1)
+        else:
+            params[k, :len(prm)] = prm
+    steps = np.ascontiguousarray(np.stack([np.asarray(s, dtype=np.float64).T.reshape(-1) for s in req.steps]))
+    r = L.Request()
+    r.dim = d
+    for i in range(d):
+        r.resolutions[i] = int(req.res[i])
+        r.lengths[i] = float((req.lengths or [1.0] * d)[i])
+    r.formulation = int(req.formulation)
+    r.flags = L.FLAG_ALLOW_EVEN
+    r.nb_materials = nm
+    r.laws = laws.ctypes.data_as(C.POINTER(C.c_int))
+    r.params = params.ctypes.data_as(C.POINTER(C.c_double))
+    r.phase = phase.ctypes.data_as(C.POINTER(C.c_ubyte))
+    if per_pixel is not None:
+        r.per_pixel = per_pixel.ctypes.data_as(C.POINTER(C.c_double))
+        r.per_pixel_stride = 2
+    r.nb_steps = len(req.steps)
+    r.load_steps = steps.ctypes.data_as(C.POINTER(C.c_double))
+    return r, (laws, params, phase, per_pixel, steps)
+
+
 def estimate_bytes(res, formulation, has_hep, precision='mixed'):
     """Device memory of one admitted request (fields, spectra, tangent data, CG
-    vectors, state), as the library allocates it."""
-    npx = int(np.prod(res))
-    d = len(res)
-    d2 = d * d
-    nk = npx // res[-1] * (res[-1] // 2 + 1)
-    b = 3 * d2 * npx * 8 + d2 * nk * 16 + 2 * d2 * npx * 8 + npx * (1 + 16) + (1 << 20)
-    if formulation == Formulation.finite_strain:
-        b += 2 * d2 * npx * 8
-    if has_hep:
-        b += 38 * npx * 8 + d2 * d * npx * 8
-    if precision == 'mixed':
-        b += npx * 8 + d2 * nk * 8 + 4 * d2 * npx * 4
-        if formulation == Formulation.finite_strain:
-            b += 2 * d2 * npx * 4
-        if has_hep:
-            b += d2 * d * npx * 4
-    else:
-        b += 4 * d2 * npx * 8
-    return int(b)
-
-
-def build_cell(req, flags=0):
-    import muspectre_gb300 as mu
-    d = len(req.res)
-    cell = Cell(req.res, req.lengths or [1.0] * d, Formulation(req.formulation), allow_even=True)
-    for k, (law, params) in enumerate(req.materials):
-        mask = req.phase == k
-        if not np.any(mask):
-            continue
-        if law == 'le1':
-            getattr(mu.material, 'MaterialLinearElastic1_%dd' % d).make(cell, 'm%d' % k, *params).add_pixels(mask)
-        elif law == 'le4':
-            E, nu = params
-            getattr(mu.material, 'MaterialLinearElastic4_%dd' % d).make(cell, 'm%d' % k).add_pixels(
-                np.flatnonzero(mask), E, nu)
-        elif law == 'hep1':
-            getattr(mu.material, 'MaterialHyperElastoPlastic1_%dd' % d).make(cell, 'm%d' % k, *params).add_pixels(mask)
-        else:
-            raise ValueError('unknown law ' + law)
-    cell.initialise(flags)
-    return cell
-
-
-def solve_alone(req, tol=1e-8, maxiter=2000, newton_tol=1e-6, precision='mixed'):
-    """The reference point of the serving test: the request on its own."""
-    cell = build_cell(req)
-    d = len(req.res)
-    try:
-        rs = _solvers.newton_cg(cell, list(req.steps), _solvers.SolverCG(cell, tol, maxiter, precision=precision),
-                                newton_tol, 0.0)
-        r = rs[-1]
-        return Result(req.rid, r.success, r.message, r.nb_it, r.nb_fev,
-                      r.stress.reshape(-1, d, d).transpose(0, 2, 1).mean(0), 0.0)
-    except _solvers.ConvergenceError as e:
-        return Result(req.rid, False, str(e)[:63], 0, 0, np.full((d, d), np.nan), 0.0)
+    vectors, state), as the library allocates it (musg_request_bytes)."""
+    r = L.Request()
+    r.dim = len(res)
+    for i, n in enumerate(res):
+        r.resolutions[i] = int(n)
+    r.formulation = int(formulation)
+    r.nb_materials = 1
+    law = (C.c_int * 1)(L.LAW_HEP1 if has_hep else L.LAW_LE1)
+    r.laws = C.cast(law, C.POINTER(C.c_int))
+    out = C.c_ulonglong(0)
+    L.check(L.lib().musg_request_bytes(C.byref(r), _PREC[precision], C.byref(out)))
+    return int(out.value)
 
 
 class Server:
-    """Admission by HBM budget, lanes on separate streams, same-shape batching."""
+    """Admission by HBM budget, native lanes on separate streams, same-shape batching.
+    ``lanes=0`` runs nothing: ``_take`` / ``_release`` then step the admission by
+    hand (host-side checks of the policy)."""
 
     def __init__(self, hbm_budget_bytes, lanes=4, max_batch=8, precision='mixed', tol=1e-8, maxiter=2000,
                  newton_tol=1e-6):
@@ -129,108 +125,95 @@ class Server:
         self.lanes = int(lanes)
         self.max_batch = int(max_batch)
         self.precision = precision
-        self.tol, self.maxiter, self.newton_tol = tol, maxiter, newton_tol
-        self.in_use = 0
-        self.peak_in_use = 0
-        self.queue: deque = deque()
         self.results: Dict[int, Result] = {}
-        self.cv = threading.Condition()
-        self.closed = False
-        self.admitted_batches = 0
-        self._threads: List[threading.Thread] = []
+        self._ids: Dict[int, tuple] = {}
+        self._by_id: Dict[int, int] = {}
+        h = C.c_void_p()
+        L.check(L.lib().musg_server_create(C.c_ulonglong(self.budget), self.lanes, self.max_batch, _PREC[precision],
+                                           float(tol), int(maxiter), float(newton_tol), C.byref(h)))
+        self._h = h
+
+    def __del__(self):
+        h = getattr(self, '_h', None)
+        if h is not None and h.value:
+            try:
+                L.lib().musg_server_destroy(h)
+            except Exception:
+                pass
+            self._h = None
 
     # ------------------------------------------------------------------ client side
     def submit(self, req: Request):
-        with self.cv:
-            req.arrival = time.perf_counter()
-            self.queue.append(req)
-            self.cv.notify_all()
+        req.arrival = time.perf_counter()
+        r, keep = _native(req)
+        nid = C.c_longlong(0)
+        L.check(L.lib().musg_server_submit(self._h, C.byref(r), C.byref(nid)))
+        self._ids[req.rid] = (int(nid.value), len(req.res))
+        self._by_id[int(nid.value)] = req.rid
+        return req.rid
 
     def close(self):
-        with self.cv:
-            self.closed = True
-            self.cv.notify_all()
+        L.check(L.lib().musg_server_close(self._h))
 
     def start(self):
-        for i in range(self.lanes):
-            t = threading.Thread(target=self._lane, name='musg-lane-%d' % i, daemon=True)
-            t.start()
-            self._threads.append(t)
+        """Lanes start with the server; kept for the call sequence of run_stream."""
 
-    def join(self):
-        for t in self._threads:
-            t.join()
+    def result(self, rid, timeout=3600.0):
+        if rid in self.results:
+            return self.results[rid]
+        nid, d = self._ids[rid]
+        out = L.ServerResult()
+        L.check(L.lib().musg_server_wait(self._h, nid, float(timeout), C.byref(out)))
+        stress = np.array(out.stress[:d * d]).reshape(d, d).T
+        res = Result(rid, bool(out.success), out.message.decode('utf-8', 'replace'), int(out.nb_it), int(out.nb_fev),
+                     stress if out.success else np.full((d, d), np.nan), float(out.latency_s),
+                     int(out.batched_with))
+        self.results[rid] = res
+        return res
 
-    # ------------------------------------------------------------------ lanes
-    def _footprint(self, req):
-        has_hep = any(m[0] == 'hep1' for m in req.materials)
-        return estimate_bytes(req.res, req.formulation, has_hep, self.precision)
+    def join(self, timeout=3600.0):
+        for rid in list(self._ids):
+            self.result(rid, timeout)
 
+    def _stats(self):
+        st = L.ServerStats()
+        L.check(L.lib().musg_server_get_stats(self._h, C.byref(st)))
+        return st
+
+    @property
+    def in_use(self):
+        return int(self._stats().in_use)
+
+    @property
+    def peak_in_use(self):
+        return int(self._stats().peak_in_use)
+
+    @property
+    def admitted_batches(self):
+        return int(self._stats().batches)
+
+    # ------------------------------------------------------------------ admission by hand
     def _take(self):
-        """Next admissible group: the oldest request that fits the budget, plus the
-        waiting requests of the same shape that also fit (continuous batching)."""
-        for i, req in enumerate(self.queue):
-            fp = self._footprint(req)
-            if self.in_use + fp > self.budget and self.in_use > 0:
-                continue
-            group = [req]
-            used = fp
-            key = req.shape_key()
-            for other in list(self.queue)[i + 1:]:
-                if len(group) >= self.max_batch:
-                    break
-                if other.shape_key() == key and self.in_use + used + fp <= self.budget:
-                    group.append(other)
-                    used += fp
-            for g in group:
-                self.queue.remove(g)
-            self.in_use += used
-            self.peak_in_use = max(self.peak_in_use, self.in_use)
-            return group, used
-        return None, 0
+        """One admission step (servers without lanes): (rids of the group, bytes)."""
+        ids = (C.c_longlong * self.max_batch)()
+        n = C.c_int(0)
+        used = C.c_ulonglong(0)
+        L.check(L.lib().musg_server_admit(self._h, ids, self.max_batch, C.byref(n), C.byref(used)))
+        if n.value == 0:
+            return None, 0
+        return [self._by_id[int(ids[k])] for k in range(n.value)], int(used.value)
 
-    def _lane(self):
-        while True:
-            with self.cv:
-                while True:
-                    group, used = self._take()
-                    if group is not None:
-                        break
-                    if self.closed and not self.queue:
-                        return
-                    self.cv.wait(0.05)
-            try:
-                self._run(group)
-            finally:
-                with self.cv:
-                    self.in_use -= used
-                    self.cv.notify_all()
+    def _release(self, used):
+        L.check(L.lib().musg_server_release(self._h, C.c_ulonglong(int(used))))
 
-    def _run(self, group):
-        d = len(group[0].res)
-        cells = [build_cell(r) for r in group]
-        res = []
-        if len(group) == 1:
-            req = group[0]
-            try:
-                rs = _solvers.newton_cg(cells[0], list(req.steps),
-                                        _solvers.SolverCG(cells[0], self.tol, self.maxiter, precision=self.precision),
-                                        self.newton_tol, 0.0)
-                res.append(rs[-1])
-            except _solvers.ConvergenceError as e:
-                res.append(_solvers.OptimizeResult(np.empty((0, 1)), np.empty((0, 1)), False, 0, str(e)[:63], 0, 0))
-        else:
-            steps = np.stack([np.stack(r.steps) for r in group])
-            bs = _batch.BatchSolver(cells, self.tol, self.maxiter, precision=self.precision)
-            out = bs.newton_cg(steps, self.newton_tol, 0.0)
-            res = [o[-1] for o in out]
-            self.admitted_batches += 1
-        now = time.perf_counter()
-        for req, r in zip(group, res):
-            st = r.stress.reshape(-1, d, d).transpose(0, 2, 1).mean(0) if r.stress.size else np.full((d, d), np.nan)
-            result = Result(req.rid, r.success, r.message, r.nb_it, r.nb_fev, st, now - req.arrival, len(group))
-            with self.cv:
-                self.results[req.rid] = result
+
+def solve_alone(req, tol=1e-8, maxiter=2000, newton_tol=1e-6, precision='mixed'):
+    """The reference point of the serving test: the request on its own (one lane,
+    no batching, nothing else running)."""
+    srv = Server(1 << 62, lanes=1, max_batch=1, precision=precision, tol=tol, maxiter=maxiter, newton_tol=newton_tol)
+    srv.submit(req)
+    srv.close()
+    return srv.result(req.rid)
 
 
 def c5_request(rid, seed, small=False):

@@ -1,5 +1,6 @@
-"""Host logic of the request server (no GPU): admission by HBM budget, same-shape
-batching, memory returned on completion, the config-5 request generator."""
+"""Host logic of the native request server (no GPU: servers without lanes run
+nothing): admission by HBM budget, same-shape batching, memory returned on
+completion, request validation, the config-5 request generator."""
 import numpy as np
 
 from muspectre_gb300 import serving
@@ -22,25 +23,54 @@ def test_estimate_bytes_grows():
 
 
 def test_admission_budget_and_batching():
+    """The native admission step (musg_server_admit on a server without lanes)."""
     fp = serving.estimate_bytes([64, 64], Formulation.finite_strain, False)
-    srv = serving.Server(hbm_budget_bytes=int(2.5 * fp), lanes=2, max_batch=4)
+    srv = serving.Server(hbm_budget_bytes=int(2.5 * fp), lanes=0, max_batch=4)
     for rid, n in enumerate([64, 64, 96, 64, 64]):
-        srv.queue.append(_req(rid, n))
+        srv.submit(_req(rid, n))
     g1, used1 = srv._take()
-    assert [r.rid for r in g1] == [0, 1]          # same shape, two fit the budget
+    assert g1 == [0, 1]                           # same shape, two fit the budget
     assert srv.in_use == used1 <= srv.budget
     g2, used2 = srv._take()                       # 96^2 does not fit next to two 64^2
     assert g2 is None or srv.in_use <= srv.budget
-    srv.in_use -= used1                           # first group completes
+    srv._release(used1)                           # first group completes
     g3, used3 = srv._take()
     assert g3 is not None and srv.in_use <= srv.budget
+    assert srv.peak_in_use <= srv.budget
 
 
 def test_oversized_request_admitted_alone():
-    srv = serving.Server(hbm_budget_bytes=1, lanes=1)
-    srv.queue.append(_req(0, 64))
+    srv = serving.Server(hbm_budget_bytes=1, lanes=0)
+    srv.submit(_req(0, 64))
     g, used = srv._take()                          # an idle server admits it anyway
-    assert g is not None and len(g) == 1 and srv.in_use == used
+    assert g == [0] and srv.in_use == used
+    g2, _ = srv._take()
+    assert g2 is None
+
+
+def test_batches_keep_shape_and_law_kind():
+    """Only requests of one shape (grid, formulation, law kind, steps) share a batch."""
+    srv = serving.Server(hbm_budget_bytes=1 << 40, lanes=0, max_batch=8)
+    srv.submit(_req(0, 64))
+    srv.submit(_req(1, 64, hep=True))
+    srv.submit(_req(2, 64))
+    srv.submit(_req(3, 80))
+    g, _ = srv._take()
+    assert g == [0, 2]
+    assert srv._take()[0] == [1]
+    assert srv._take()[0] == [3]
+
+
+def test_request_validation():
+    import pytest
+    srv = serving.Server(hbm_budget_bytes=1 << 30, lanes=0)
+    bad = _req(0, 16)
+    bad.phase = np.full(16 * 16, 3)               # material index beyond the list
+    with pytest.raises(ValueError):
+        srv.submit(bad)
+    srv.close()
+    with pytest.raises(RuntimeError):
+        srv.submit(_req(1, 16))
 
 
 def test_c5_generator_ranges():
