@@ -145,6 +145,25 @@ int musg_cell_directional_stiffness(musg_cell *cell, const double *dF, double *d
 int musg_cell_cg_operator(musg_cell *cell, int precision, const double *dF, double *dP);
 /* Cell::save_history_variables (cell_base.cc:458-462) */
 int musg_cell_save_history_variables(musg_cell *cell);
+/* CellBase::get_globalised_internal_real_array (cell_base.cc:370-436): the internal
+ * field `name` of the materials that have it, zero at the other pixels; host array
+ * of nb_components values per pixel (pixel-major).  Names as in the reference:
+ * "Eigenstrain" (LE2), "local stiffness tensor" (LE3), "local first Lame constant",
+ * "local second Lame constant(shear modulus)" (LE4), and the HEP1 state fields
+ * "cumulated plastic flow εₚ, sub_field index k", "Previous placement gradient Fᵗ,
+ * sub_field index k", "Previous left Cauchy-Green deformation bₑᵗ, sub_field index k"
+ * (k = 0, 1; the current one alternates with save_history_variables).  out = NULL
+ * returns nb_components only. */
+int musg_cell_get_internal(musg_cell *cell, const char *name, double *out, long long capacity,
+                           int *nb_components);
+/* checkpoint / resume of a cell's device state at a load-step boundary (no
+ * counterpart in the reference): strain and stress fields and the elasto-plastic
+ * state with its current/old index, as one host image.  Loading needs a cell of the
+ * same grid, formulation and material kinds (built the same way); its tangent is
+ * re-evaluated by the next solve. */
+int musg_cell_checkpoint_size(musg_cell *cell, unsigned long long *bytes);
+int musg_cell_checkpoint_save(musg_cell *cell, void *buf, unsigned long long bytes);
+int musg_cell_checkpoint_load(musg_cell *cell, const void *buf, unsigned long long bytes);
 
 /* -------------------------------------------------------------- solvers
  * SolverCG(cell, tol, maxiter, verbose) (src/solver/solver_cg.hh:51-106) with the

@@ -92,6 +92,10 @@ _SIGNATURES = {
     'musg_cell_cg_operator': (C.c_int, [_P, C.c_int, _D, _D]),
     'musg_cell_save_history_variables': (C.c_int, [_P]),
     'musg_cell_homogenised_stress': (C.c_int, [_P, _D]),
+    'musg_cell_get_internal': (C.c_int, [_P, C.c_char_p, _D, C.c_longlong, _I]),
+    'musg_cell_checkpoint_size': (C.c_int, [_P, C.POINTER(C.c_ulonglong)]),
+    'musg_cell_checkpoint_save': (C.c_int, [_P, _P, C.c_ulonglong]),
+    'musg_cell_checkpoint_load': (C.c_int, [_P, _P, C.c_ulonglong]),
     'musg_solver_cg_create': (C.c_int, [_P, C.c_double, C.c_uint, C.c_int, C.c_int, C.POINTER(_P)]),
     'musg_solver_destroy': (C.c_int, [_P]),
     'musg_solver_set_inner_tol': (C.c_int, [_P, C.c_double]),

@@ -262,6 +262,54 @@ class CellBase:
         L.check(L.lib().musg_cell_cg_operator(self._h, prec, L.dptr(v), L.dptr(out)))
         return self._to_array(out)
 
+    def get_globalised_internal_real_array(self, unique_name):
+        """CellBase::get_globalised_internal_real_array (cell_base.cc:370-436): the
+        internal field of the materials that have it, zeros elsewhere, as a
+        (nb_components, nb_pixels) array.  RuntimeError when no material has it."""
+        self.initialise()
+        name = unique_name.encode('utf-8')
+        nc = C.c_int(0)
+        L.check(L.lib().musg_cell_get_internal(self._h, name, None, 0, C.byref(nc)))
+        out = np.empty(self.nb_pixels * nc.value)
+        L.check(L.lib().musg_cell_get_internal(self._h, name, L.dptr(out), out.size, C.byref(nc)))
+        return out.reshape(self.nb_pixels, nc.value).T
+
+    def get_managed_real_array(self, unique_name, nb_components):
+        """CellBase::get_managed_real_array (cell_base.cc:419-427): a cell-owned
+        (nb_components, nb_pixels) array, created on first use; asking again with
+        another number of components raises RuntimeError (cell_base.cc:354-363)."""
+        managed = self.__dict__.setdefault('_managed', {})
+        a = managed.get(unique_name)
+        if a is None:
+            a = managed[unique_name] = np.zeros((int(nb_components), self.nb_pixels))
+        elif a.shape[0] != int(nb_components):
+            raise RuntimeError("Field '{}' already exists and it has {} components. You asked for a field with "
+                               "{}components.".format(unique_name, a.shape[0], nb_components))
+        return a
+
+    def checkpoint(self):
+        """The cell's device state (strain, stress, elasto-plastic state) as bytes, for
+        restore() into a cell built the same way (an extension of the reference)."""
+        self.initialise()
+        n = C.c_ulonglong(0)
+        L.check(L.lib().musg_cell_checkpoint_size(self._h, C.byref(n)))
+        buf = C.create_string_buffer(n.value)
+        L.check(L.lib().musg_cell_checkpoint_save(self._h, buf, n))
+        return buf.raw
+
+    def restore(self, image):
+        """Load a checkpoint() image; the next solve continues from its state."""
+        self.initialise()
+        buf = C.create_string_buffer(bytes(image), len(image))
+        L.check(L.lib().musg_cell_checkpoint_load(self._h, buf, len(image)))
+        self._has_tangent = False
+
+    def homogenised_stress(self):
+        """Pixel mean of the stress field (D×D), reduced on the device."""
+        out = np.empty(self.dim * self.dim)
+        L.check(L.lib().musg_cell_homogenised_stress(self._h, L.dptr(out)))
+        return out.reshape(self.dim, self.dim).T
+
     def save_history_variables(self):
         L.check(L.lib().musg_cell_save_history_variables(self._h))
 

@@ -1257,6 +1257,168 @@ int musg_cell_save_history_variables(musg_cell *cell) {
   });
 }
 
+int musg_cell_get_internal(musg_cell *cell, const char *name, double *out, long long capacity, int *nb_components) {
+  return guard([&] {
+    require(cell && name, MUSG_ERR_ARGUMENT, "null argument");
+    musg_cell &c = *cell;
+    const int D = c.dim, D2 = c.D2;
+    // the internal fields of the reference's materials and where their values live
+    enum Src { EIG, CT4, LAM, MU, EPS, FPREV, BE };
+    struct Spec {
+      int law, ncomp, src, slot;
+    } sp{0, 0, 0, 0};
+    const std::string n = name;
+    const std::string sub = ", sub_field index ";
+    // HEP1 state fields (material_hyper_elasto_plastic1.cc:46-53), two sub-fields
+    // each (statefield.hh:181-188)
+    const char *hep_prefix[3] = {"cumulated plastic flow \xce\xb5\xe2\x82\x9a",
+                                 "Previous placement gradient F\xe1\xb5\x97",
+                                 "Previous left Cauchy-Green deformation b\xe2\x82\x91\xe1\xb5\x97"};
+    bool found = false;
+    if (n == "Eigenstrain") sp = {MUSG_LAW_LE2, D2, EIG, 0}, found = true;             // material_linear_elastic2.cc:44
+    else if (n == "local stiffness tensor") sp = {MUSG_LAW_LE3, D2 * D2, CT4, 0}, found = true;  // ..._elastic3.cc:45
+    else if (n == "local first Lame constant") sp = {MUSG_LAW_LE4, 1, LAM, 0}, found = true;    // ..._elastic4.cc:47
+    else if (n == "local second Lame constant(shear modulus)") sp = {MUSG_LAW_LE4, 1, MU, 0}, found = true;
+    for (int k = 0; k < 3 && !found; ++k)
+      for (int slot = 0; slot < 2 && !found; ++slot)
+        if (n == std::string(hep_prefix[k]) + sub + std::to_string(slot)) {
+          sp = {MUSG_LAW_HEP1, k == 0 ? 1 : D2, k == 0 ? EPS : k == 1 ? FPREV : BE, slot};
+          found = true;
+        }
+    bool owned = false;
+    for (const Material &mt : c.materials) owned = owned || (found && mt.law == sp.law);
+    require(owned, MUSG_ERR_RUNTIME,
+            "The field named '" + n + "' does not exist in any of the materials and can therefore not be globalised!");
+    if (nb_components) *nb_components = sp.ncomp;
+    if (!out) return;
+    require(capacity >= (long long)sp.ncomp * c.npx, MUSG_ERR_SHAPE, "output array too small");
+    if (!c.initialised) c.initialise();
+    // the device planes behind the field
+    std::vector<const double *> planes;
+    auto field = [&](const DevBuf &b, int nplanes) {
+      for (int k = 0; k < nplanes; ++k) planes.push_back(b.as<double>() + (size_t)k * c.npx);
+    };
+    switch (sp.src) {
+      case EIG: field(c.eig, D2); break;
+      case CT4:
+      case LAM: field(c.lam64, 1); if (sp.src == CT4) field(c.mu64, 1); break;
+      case MU: field(c.mu64, 1); break;
+      case EPS: field(c.eps[sp.slot], 1); break;
+      case FPREV: field(c.Fprev[sp.slot], D2); break;
+      default: field(c.be[sp.slot], D2); break;
+    }
+    std::vector<double> h(planes.size() * (size_t)c.npx);
+    MUSG_CUDA(cudaStreamSynchronize(c.stream));
+    for (size_t k = 0; k < planes.size(); ++k)
+      MUSG_CUDA(cudaMemcpy(h.data() + k * c.npx, planes[k], c.plane_bytes(), cudaMemcpyDeviceToHost));
+    std::fill(out, out + (size_t)sp.ncomp * c.npx, 0.0);
+    for (const Material &mt : c.materials) {
+      if (mt.law != sp.law) continue;
+      for (long long p : mt.pixels) {
+        double *o = out + (size_t)p * sp.ncomp;
+        if (sp.src == CT4) {
+          // C = lam I (x) I + 2 mu I_sym (materials_toolbox.hh:638-652), T4 layout
+          const double lam = h[p], mu = h[c.npx + p];
+          for (int l = 0; l < D; ++l)
+            for (int k = 0; k < D; ++k)
+              for (int j = 0; j < D; ++j)
+                for (int i = 0; i < D; ++i)
+                  o[(i + D * j) + D2 * (k + D * l)] =
+                      (i == j && k == l ? lam : 0.0) + mu * ((i == k && j == l ? 1.0 : 0.0) + (i == l && j == k ? 1.0 : 0.0));
+        } else {
+          for (int q = 0; q < sp.ncomp; ++q) o[q] = h[(size_t)q * c.npx + p];
+        }
+      }
+    }
+  });
+}
+
+namespace {
+// checkpoint image: header, then the strain and stress fields and (HEP1) the six
+// state planes sets, all as stored on the device (component planes)
+struct CheckpointHeader {
+  char magic[8];
+  int dim, res[3], form, has_hep, hep_cur, nbufs;
+  long long npx;
+};
+std::vector<std::pair<DevBuf *, size_t>> checkpoint_buffers(musg_cell &c) {
+  std::vector<std::pair<DevBuf *, size_t>> b{{&c.F, c.field_bytes()}, {&c.P, c.field_bytes()}};
+  if (c.has_hep)
+    for (int k = 0; k < 2; ++k) {
+      b.push_back({&c.Fprev[k], c.field_bytes()});
+      b.push_back({&c.be[k], c.field_bytes()});
+      b.push_back({&c.eps[k], c.plane_bytes()});
+    }
+  return b;
+}
+}  // namespace
+
+int musg_cell_checkpoint_size(musg_cell *cell, unsigned long long *bytes) {
+  return guard([&] {
+    require(cell && bytes, MUSG_ERR_ARGUMENT, "null argument");
+    if (!cell->initialised) cell->initialise();
+    unsigned long long b = sizeof(CheckpointHeader);
+    for (auto &e : checkpoint_buffers(*cell)) b += e.second;
+    *bytes = b;
+  });
+}
+
+int musg_cell_checkpoint_save(musg_cell *cell, void *buf, unsigned long long bytes) {
+  return guard([&] {
+    require(cell && buf, MUSG_ERR_ARGUMENT, "null argument");
+    musg_cell &c = *cell;
+    if (!c.initialised) c.initialise();
+    auto bufs = checkpoint_buffers(c);
+    unsigned long long need = sizeof(CheckpointHeader);
+    for (auto &e : bufs) need += e.second;
+    require(bytes >= need, MUSG_ERR_SHAPE, "checkpoint buffer too small");
+    CheckpointHeader h{};
+    memcpy(h.magic, "MUSGCKP1", 8);
+    h.dim = c.dim;
+    for (int d = 0; d < 3; ++d) h.res[d] = c.res[d];
+    h.form = c.form;
+    h.has_hep = c.has_hep;
+    h.hep_cur = c.hep_cur;
+    h.nbufs = (int)bufs.size();
+    h.npx = c.npx;
+    char *o = (char *)buf;
+    memcpy(o, &h, sizeof(h));
+    o += sizeof(h);
+    MUSG_CUDA(cudaStreamSynchronize(c.stream));
+    for (auto &e : bufs) {
+      MUSG_CUDA(cudaMemcpy(o, e.first->p, e.second, cudaMemcpyDeviceToHost));
+      o += e.second;
+    }
+  });
+}
+
+int musg_cell_checkpoint_load(musg_cell *cell, const void *buf, unsigned long long bytes) {
+  return guard([&] {
+    require(cell && buf, MUSG_ERR_ARGUMENT, "null argument");
+    musg_cell &c = *cell;
+    if (!c.initialised) c.initialise();
+    require(bytes >= sizeof(CheckpointHeader), MUSG_ERR_SHAPE, "checkpoint too short");
+    CheckpointHeader h;
+    memcpy(&h, buf, sizeof(h));
+    require(memcmp(h.magic, "MUSGCKP1", 8) == 0, MUSG_ERR_ARGUMENT, "not a cell checkpoint");
+    auto bufs = checkpoint_buffers(c);
+    require(h.dim == c.dim && h.res[0] == c.res[0] && h.res[1] == c.res[1] && h.res[2] == c.res[2] &&
+                h.form == c.form && h.has_hep == (int)c.has_hep && h.npx == c.npx && h.nbufs == (int)bufs.size(),
+            MUSG_ERR_SHAPE, "the checkpoint belongs to a cell of another shape or material kind");
+    unsigned long long need = sizeof(CheckpointHeader);
+    for (auto &e : bufs) need += e.second;
+    require(bytes >= need, MUSG_ERR_SHAPE, "checkpoint too short");
+    const char *i = (const char *)buf + sizeof(h);
+    MUSG_CUDA(cudaStreamSynchronize(c.stream));
+    for (auto &e : bufs) {
+      MUSG_CUDA(cudaMemcpy(e.first->p, i, e.second, cudaMemcpyHostToDevice));
+      i += e.second;
+    }
+    c.hep_cur = h.hep_cur;
+    c.tangent_valid = false;  // re-evaluated at the restored strain by the next solve
+  });
+}
+
 int musg_solver_cg_create(musg_cell *cell, double tol, unsigned maxiter, int verbose, int precision,
                           musg_solver **out) {
   return guard([&] {
