@@ -190,6 +190,15 @@ int musg_newton_cg(musg_cell *cell, const double *load_steps, int nb_steps,
                    int verbose, musg_result_info *infos, double *grads,
                    double *stresses);
 
+/* de_geus(cell, load_steps, solver, newton_tol, equil_tol, verbose)
+ * (src/solver/solvers.cc:220-408): per load step, the first Newton iteration solves
+ * for the response to the macroscopic increment at the previous equilibrium
+ * (rhs = -G(K:DF)); arguments and outputs as musg_newton_cg. */
+int musg_de_geus(musg_cell *cell, const double *load_steps, int nb_steps,
+                 musg_solver *solver, double newton_tol, double equil_tol,
+                 int verbose, musg_result_info *infos, double *grads,
+                 double *stresses);
+
 /* -------------------------------------------------------------- batches
  * Many same-shape cells (RVEs, or right-hand sides on copies of one microstructure)
  * solved together: newton_cg's Newton steps run in lockstep per cell and every CG

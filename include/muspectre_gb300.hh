@@ -404,6 +404,34 @@ inline std::vector<OptimizeResult> newton_cg(Cell &cell, const std::vector<std::
   return out;
 }
 
+// de_geus (solvers.cc:220-408), same arguments and results as newton_cg
+inline std::vector<OptimizeResult> de_geus(Cell &cell, const std::vector<std::vector<Real>> &load_steps,
+                                           SolverCG &solver, Real newton_tol, Real equil_tol, Dim_t verbose = 0) {
+  const int D2 = cell.get_dim() * cell.get_dim();
+  std::vector<Real> flat;
+  for (const auto &s : load_steps) {
+    if (int(s.size()) != D2) throw SolverError("Load increments need to be given in D×D matrices");
+    flat.insert(flat.end(), s.begin(), s.end());
+  }
+  const int n = int(load_steps.size());
+  std::vector<musg_result_info> infos(n);
+  const size_t nd = size_t(cell.get_nb_dof());
+  std::vector<Real> grads(n * nd), stresses(n * nd);
+  check(musg_de_geus(cell.handle(), flat.data(), n, solver.handle(), newton_tol, equil_tol, verbose, infos.data(),
+                     grads.data(), stresses.data()));
+  std::vector<OptimizeResult> out(n);
+  for (int k = 0; k < n; ++k) {
+    out[k].success = infos[k].success != 0;
+    out[k].status = infos[k].status;
+    out[k].message = infos[k].message;
+    out[k].nb_it = infos[k].nb_it;
+    out[k].nb_fev = infos[k].nb_fev;
+    out[k].grad.assign(grads.begin() + k * nd, grads.begin() + (k + 1) * nd);
+    out[k].stress.assign(stresses.begin() + k * nd, stresses.begin() + (k + 1) * nd);
+  }
+  return out;
+}
+
 // the single-load overload (solvers.hh:65-74)
 inline OptimizeResult newton_cg(Cell &cell, const std::vector<Real> &delF0, SolverCG &solver, Real newton_tol,
                                 Real equil_tol, Dim_t verbose = 0) {

@@ -105,6 +105,8 @@ _SIGNATURES = {
     'musg_solver_solve': (C.c_int, [_P, _D, _D]),
     'musg_newton_cg': (C.c_int, [_P, _D, C.c_int, _P, C.c_double, C.c_double, C.c_int, C.POINTER(ResultInfo), _D,
                                  _D]),
+    'musg_de_geus': (C.c_int, [_P, _D, C.c_int, _P, C.c_double, C.c_double, C.c_int, C.POINTER(ResultInfo), _D,
+                               _D]),
     'musg_batch_create': (C.c_int, [C.POINTER(_P), C.c_int, C.c_double, C.c_uint, C.c_int, C.POINTER(_P)]),
     'musg_batch_destroy': (C.c_int, [_P]),
     'musg_batch_set_inner_tol': (C.c_int, [_P, C.c_double]),

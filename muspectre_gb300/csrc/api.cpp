@@ -770,8 +770,12 @@ void check_symmetry_or_throw(const double *m, int dim) {
   if (!(rel >= a / n || rel >= n)) throw Error(MUSG_ERR_SOLVER, "all Δε must be symmetric!");
 }
 
+// newton_cg (solvers.cc:44-217), or with geus the de Geus variant (solvers.cc:220-408):
+// per load step its first Newton iteration solves K dF = -G(K:DF) at the previous
+// equilibrium and then applies DF + dF (DF: the macroscopic increment as a field)
 void newton_cg_impl(musg_cell *cell, const double *steps, int nsteps, musg_solver *solver, double newton_tol,
-                    double equil_tol, int verbose, musg_result_info *infos, double *grads, double *stresses) {
+                    double equil_tol, int verbose, musg_result_info *infos, double *grads, double *stresses,
+                    bool geus = false) {
   require(cell && solver && steps && nsteps > 0, MUSG_ERR_ARGUMENT, "invalid newton_cg arguments");
   require(solver->cell == cell, MUSG_ERR_ARGUMENT, "solver belongs to another cell");
   musg_cell &c = *cell;
@@ -786,7 +790,7 @@ void newton_cg_impl(musg_cell *cell, const double *steps, int nsteps, musg_solve
     for (int k = 0; k < nsteps; ++k) check_symmetry_or_throw(steps + (size_t)k * D2, dim);
   fill_uniform(c.F.as<double>(), c.put_matrix(I.data(), 0), D2, c.npx, s);
   if (verbose > 0) {
-    printf("Newton-CG for %s strain with\nnewton_tol = %g, cg_tol = %g maxiter = %u\n",
+    printf("%s for %s strain with\nnewton_tol = %g, cg_tol = %g maxiter = %u\n", geus ? "de Geus-CG" : "Newton-CG",
            c.form == MUSG_FINITE_STRAIN ? "finite" : "small", newton_tol, solver->tol, solver->maxiter);
   }
   std::vector<double> previous(D2, 0.0);
@@ -796,7 +800,8 @@ void newton_cg_impl(musg_cell *cell, const double *steps, int nsteps, musg_solve
     const double *macro = steps + (size_t)step * D2;
     std::vector<double> delta(D2);
     for (int k = 0; k < D2; ++k) delta[k] = macro[k] - previous[k];
-    add_macro(c.F.as<double>(), c.put_matrix(delta.data(), 16), D2, c.npx, s);
+    double *ddelta = c.put_matrix(delta.data(), 16);
+    if (!geus) add_macro(c.F.as<double>(), ddelta, D2, c.npx, s);
     std::string message = "Has not converged";
     double incr_norm = 2 * newton_tol, grad_norm = 1, stress_norm = 2 * equil_tol;
     bool has_converged = false;
@@ -811,14 +816,23 @@ void newton_cg_impl(musg_cell *cell, const double *steps, int nsteps, musg_solve
     unsigned newt_iter = 0;
     for (; newt_iter < solver->maxiter && !has_converged; ++newt_iter) {
       c.evaluate(false);
-      // rhs = -P, projected (FP64)
-      spectral_project<double>(c.sp, c.P.as<double>(), c.rhs.as<double>(), -1.0, s);
+      const bool first_geus = geus && newt_iter == 0;
+      if (first_geus) {
+        // rhs = -G(K:DF) with DF the uniform macroscopic increment (FP64)
+        fill_uniform(c.rhs.as<double>(), ddelta, D2, c.npx, s);
+        tangent_operator<double>(c.sp, c.tkind, c.tangent<double>(), c.rhs.as<double>(), c.rhs.as<double>(), s);
+        convert<double, double>(c.rhs.as<double>(), c.rhs.as<double>(), n, -1.0, s);
+      } else {
+        // rhs = -P, projected (FP64)
+        spectral_project<double>(c.sp, c.P.as<double>(), c.rhs.as<double>(), -1.0, s);
+      }
       dot_device<double, double>(c.rhs.as<double>(), c.rhs.as<double>(), n, c.partial.as<double>(), dscal + 32, s);
       MUSG_CUDA(cudaMemcpyAsync(c.hscal + 32, dscal + 32, sizeof(double), cudaMemcpyDeviceToHost, s));
       MUSG_CUDA(cudaStreamSynchronize(s));
       stress_norm = std::sqrt(c.hscal[32]);
       if (convergence_test()) break;
       solver->solve_device_any(c.rhs.as<double>());
+      if (first_geus) add_macro(c.F.as<double>(), ddelta, D2, c.npx, s);
       if (solver->precision == MUSG_PRECISION_MIXED)
         newton_update<float>(c.F.as<double>(), solver->x.as<float>(), n, c.partial.as<double>(), dscal + 34, s);
       else
@@ -1560,6 +1574,13 @@ int musg_newton_cg(musg_cell *cell, const double *load_steps, int nb_steps, musg
                    double equil_tol, int verbose, musg_result_info *infos, double *grads, double *stresses) {
   return guard([&] {
     newton_cg_impl(cell, load_steps, nb_steps, solver, newton_tol, equil_tol, verbose, infos, grads, stresses);
+  });
+}
+
+int musg_de_geus(musg_cell *cell, const double *load_steps, int nb_steps, musg_solver *solver, double newton_tol,
+                 double equil_tol, int verbose, musg_result_info *infos, double *grads, double *stresses) {
+  return guard([&] {
+    newton_cg_impl(cell, load_steps, nb_steps, solver, newton_tol, equil_tol, verbose, infos, grads, stresses, true);
   });
 }
 

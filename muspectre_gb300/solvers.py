@@ -118,6 +118,17 @@ def newton_cg(cell, load_steps, solver, newton_tol, equil_tol=None, verbose=0, *
     (bind_py_solvers.cc:75-106).  A single D×D load returns one OptimizeResult, a
     list returns a list.  ``return_fields=False`` skips the per-step copies of the
     strain and stress fields to the host (the arrays are then empty)."""
+    return _newton('musg_newton_cg', cell, load_steps, solver, newton_tol, equil_tol, verbose, return_fields, kw)
+
+
+def de_geus(cell, load_steps, solver, newton_tol, equil_tol=None, verbose=0, *, return_fields=True, **kw):
+    """de_geus(cell, ΔF₀ | [ΔF...], solver, newton_tol, equil_tol, verbose=0)
+    (bind_py_solvers.cc:108-138, solvers.cc:220-408): each load step starts with the
+    response to the macroscopic increment at the previous equilibrium."""
+    return _newton('musg_de_geus', cell, load_steps, solver, newton_tol, equil_tol, verbose, return_fields, kw)
+
+
+def _newton(entry, cell, load_steps, solver, newton_tol, equil_tol, verbose, return_fields, kw):
     if equil_tol is None:
         equil_tol = kw.pop('equilibrium_tol')
     single = not isinstance(load_steps, (list, tuple))
@@ -134,8 +145,8 @@ def newton_cg(cell, load_steps, solver, newton_tol, equil_tol=None, verbose=0, *
     infos = (L.ResultInfo * n)()
     grads = np.empty((n, cell.nb_dof)) if return_fields else None
     stresses = np.empty((n, cell.nb_dof)) if return_fields else None
-    L.check(L.lib().musg_newton_cg(cell.handle, L.dptr(flat), n, solver.handle, float(newton_tol), float(equil_tol),
-                                   int(verbose), infos, L.dptr(grads), L.dptr(stresses)))
+    L.check(getattr(L.lib(), entry)(cell.handle, L.dptr(flat), n, solver.handle, float(newton_tol), float(equil_tol),
+                                    int(verbose), infos, L.dptr(grads), L.dptr(stresses)))
     cell._has_tangent = True
     out = []
     for k in range(n):

@@ -874,6 +874,78 @@ def newton_cg(cell, load_steps, solver, newton_tol, equil_tol, verbose=0):
     return results[0] if single else results
 
 
+def de_geus(cell, load_steps, solver, newton_tol, equil_tol, verbose=0):
+    """solvers.cc:220-408: Newton-Krylov of de Geus et al. (2017).  Per load step the
+    first Newton iteration solves K δF = -G(K:ΔF̄) at the previous equilibrium
+    (:343-355) and then applies ΔF̄ + δF; later iterations are those of newton_cg."""
+    single = isinstance(load_steps, np.ndarray) and load_steps.ndim == 2
+    steps = [np.asarray(load_steps, dtype=float)] if single else [np.asarray(s, dtype=float) for s in load_steps]
+    d = cell.dim
+    solver.initialise()
+    if cell.form == FINITE_STRAIN:
+        cell.set_uniform_strain(np.eye(d))
+        for s in steps:
+            if s.shape != (d, d):
+                raise SolverError("Load increments need to be given in %d×%d matrices" % (d, d))
+    elif cell.form == SMALL_STRAIN:
+        cell.set_uniform_strain(np.zeros((d, d)))
+        for s in steps:
+            if s.shape != (d, d):
+                raise SolverError("Load increments need to be given in %d×%d matrices" % (d, d))
+            if not check_symmetry(s):
+                raise SolverError("all Δε must be symmetric!")
+    else:
+        raise SolverError("Unknown strain measure")
+
+    results = []
+    previous = np.zeros((d, d))
+    for macro in steps:
+        incr_norm, grad_norm = 2 * newton_tol, 1.0
+        stress_norm = 2 * equil_tol
+        state = {'conv': False, 'msg': "Has not converged"}
+
+        def convergence_test():
+            incr_test = incr_norm / grad_norm <= newton_tol
+            stress_test = stress_norm < equil_tol
+            if incr_test:
+                state['msg'] = "Residual  tolerance reached"
+            elif stress_test:
+                state['msg'] = "Reached stress divergence tolerance"
+            state['conv'] = incr_test or stress_test
+            return state['conv']
+
+        newt_iter = 0
+        while newt_iter < solver.get_maxiter() and not state['conv']:
+            P, _ = cell.evaluate_stress_tangent()
+            if newt_iter == 0:
+                DeltaF = t2_to_vec(np.broadcast_to(macro - previous, (cell.n_px, d, d)).copy())
+                rhs = -cell.evaluate_projected_directional_stiffness(DeltaF)
+                stress_norm = math.sqrt(float(rhs @ rhs))
+                if convergence_test():
+                    break
+                incrF = solver.solve(rhs)
+                cell.F = cell.F + DeltaF
+            else:
+                rhs = cell.apply_projection(-P)
+                stress_norm = math.sqrt(float(rhs @ rhs))
+                if convergence_test():
+                    break
+                incrF = solver.solve(rhs)
+            cell.F = cell.F + incrF
+            incr_norm = math.sqrt(float(incrF @ incrF))
+            grad_norm = math.sqrt(float(cell.F @ cell.F))
+            if verbose > 0:
+                print("at Newton step %d, |δF|/|ΔF| = %.17g, tol = %g" % (newt_iter, incr_norm / grad_norm, newton_tol))
+            convergence_test()
+            newt_iter += 1
+        previous = macro
+        conv = convergence_test()
+        results.append(OptimizeResult(cell.F.copy().reshape(-1, 1), cell.P.copy().reshape(-1, 1), conv, int(conv),
+                                      state['msg'], newt_iter, solver.get_counter()))
+        cell.save_history_variables()
+    return results[0] if single else results
+
+
 def homogenised(vec, dim):
     """Pixel mean of a flat AoS field as a D×D matrix (FP64)."""
     return t2_from_vec(np.asarray(vec, dtype=float).reshape(-1), dim).mean(axis=0)

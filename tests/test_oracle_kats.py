@@ -146,6 +146,36 @@ def test_laminate_patch():
         assert r.success
 
 
+
+def test_laminate_patch_de_geus():
+    """test_solver_newton_cg.cc:218-323 with de_geus (the pure-shear case there runs
+    de_geus, :310-323): exact layer strains to 1e-12 for both load patterns."""
+    cell, res = _laminate_cell()
+    factor = 1 / 2 * 1 / 3 + 1. - 1 / 3.
+    eps_soft = 1.0 / factor
+    eps_hard = eps_soft / 2
+    for pattern in (np.array([[1., 0], [0, 0]]), np.array([[0, 1.], [1., 0]])):
+        solver = o.SolverCG(cell, 1e-8, 2 * 10)
+        r = o.de_geus(cell, pattern, solver, 1e-5, 1e-10, 0)
+        F = o.t2_from_vec(cell.F, 2)
+        for i in range(cell.n_px):
+            ref = (eps_hard if o.get_ccoord(res, i)[0] < 1 else eps_soft) * pattern
+            assert np.linalg.norm(F[i] - ref) <= TOL
+        assert r.success
+
+
+def test_de_geus_first_step_is_the_increment_response():
+    """solvers.cc:343-355: the first de Geus iteration solves K dF = -G(K:DF) at the
+    previous equilibrium; on a linear cell de_geus and newton_cg reach the same
+    strain field."""
+    cell, res = _laminate_cell()
+    load = np.array([[0.3, 0.1], [0.1, -0.2]])
+    rg = o.de_geus(cell, load, o.SolverCG(cell, 1e-12, 40), 1e-8, 0.0, 0)
+    Fg = cell.F.copy()
+    rn = o.newton_cg(cell, load, o.SolverCG(cell, 1e-12, 40), 1e-8, 0.0, 0)
+    assert rg.success and rn.success
+    assert np.abs(Fg - cell.F).max() < 1e-10
+
 def test_le4_homogeneous_solve():
     """python_material_linear_elastic4_test.py:63-86: σ = 2μΔε on a homogeneous 7×7."""
     cell = o.Cell([7, 7], [2.3, 3.9], o.SMALL_STRAIN)
