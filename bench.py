@@ -57,6 +57,7 @@ def parse():
     ap.add_argument('--e2e-steps', type=int, default=2)
     ap.add_argument('--cpu-cg-iters', type=int, default=4)
     ap.add_argument('--no-cpu', action='store_true')
+    ap.add_argument('--no-extra', action='store_true', help='skip the other workloads (configs) of the metric')
     ap.add_argument('--only', default='all', choices=['all', 'mixed'],
                     help="'mixed': the mixed-precision solves only (for profiler launch lists)")
     return ap.parse_args()
@@ -181,6 +182,80 @@ def cpu_baseline(w, newton_steps, cg_iters, nit):
                       '%d Newton steps and %d CG iterations per solve' % (nit, w['res'][0], newton_steps, cg_iters)}
 
 
+def extra_configs(mu, workloads):
+    """The other workloads of the metric, each measured once on this GPU (N=1 only):
+    README case in FP64; 256^3 lognormal LE4 with six load cases batched; 64^3
+    two-phase HEP1 (the reference method's outcome); a Poisson request stream through
+    the continuous-batching server (solves/s, p50/p99 latency)."""
+    import torch
+    from muspectre_gb300 import serving
+    out = {}
+    # README example, FP64 (the reference's own CPU-runnable case)
+    w = workloads.readme_disc()
+    times = []
+    for _ in range(3):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        cell = mu.SystemFactory(w['res'], w['lengths'], mu.Formulation.small_strain)
+        mu.material.MaterialLinearElastic1_2d.make(cell, 'hard', w['E_hard'], w['nu']).add_pixels(w['hard'])
+        mu.material.MaterialLinearElastic1_2d.make(cell, 'soft', w['E_soft'], w['nu']).add_pixels(~w['hard'])
+        r = mu.solvers.newton_cg(cell, w['load'], mu.solvers.SolverCG(cell, w['cg_tol'], w['maxiter']),
+                                 w['newton_tol'], w['equil_tol'])
+        hs = cell.homogenised_stress()
+        times.append(time.perf_counter() - t0)
+    out['readme_51x51_fp64'] = {'ms_per_solve': 1e3 * statistics.median(times[1:]), 'newton_steps': r.nb_it,
+                                'cg_iters': r.nb_fev, 'success': bool(r.success),
+                                'hom_stress': [float(x) for x in hs.reshape(-1)],
+                                'includes': 'cell construction, upload, solve, homogenised stress'}
+    # 256^3 small-strain LE4, six unit load cases batched (one launch per pass for all)
+    w = workloads.lognormal(256)
+    cells = []
+    for _ in w['loads']:
+        c = mu.Cell(w['res'], w['lengths'], mu.Formulation.small_strain, allow_even=True)
+        mu.material.MaterialLinearElastic4_3d.make(c, 'm').add_pixels(np.arange(c.nb_pixels), w['E'], w['nu'])
+        c.initialise(mu.FFT_PlanFlags.measure)
+        cells.append(c)
+    bs = mu.batch.BatchSolver(cells, w['cg_tol'], w['maxiter'], precision='mixed')
+    loads = np.stack(w['loads'])[:, None]
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    res = bs.newton_cg(loads, w['newton_tol'], w['equil_tol'], return_stress=False)
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    cg = [r[0].nb_fev for r in res]
+    npx = cells[0].nb_pixels
+    out['lognormal256_le4_6rhs_mixed'] = {
+        'seconds': dt, 'rhs_solves_per_s': len(cells) / dt, 'cg_iters_per_rhs': cg,
+        'pxit_per_s': npx * sum(cg) / dt, 'success': all(r[0].success for r in res),
+        'hom_stress_rhs0': [float(x) for x in cells[0].homogenised_stress().reshape(-1)],
+        'includes': 'first batched solve (CUDA-graph capture included), cells resident'}
+    del bs, cells
+    # 64^3 HEP1 on a two-phase Voronoi, F11 ramp in 20 steps
+    w = workloads.voronoi(64)
+    cell = mu.Cell(w['res'], w['lengths'], mu.Formulation.finite_strain, allow_even=True)
+    for ph, mask in (('A', w['phaseA']), ('B', ~w['phaseA'])):
+        p = w[ph]
+        mu.material.MaterialHyperElastoPlastic1_3d.make(cell, ph, p['E'], p['nu'], p['tau_y0'], p['H']).add_pixels(mask)
+    t0 = time.perf_counter()
+    try:
+        rs = mu.solvers.newton_cg(cell, w['steps'], mu.solvers.SolverCG(cell, w['cg_tol'], 400, precision='mixed'),
+                                  w['newton_tol'], w['equil_tol'], return_fields=False)
+        status = 'solved %d steps' % len(rs)
+    except mu.ConvergenceError as e:
+        status = 'ConvergenceError: ' + str(e)[:90]
+    out['voronoi64_hep1_20steps'] = {
+        'status': status, 'seconds': time.perf_counter() - t0,
+        'note': 'the reference method (projector logm, j-independent Kirchhoff tangent) does not solve this '
+                'configuration; the oracle and the FP64 GPU path end the same way'}
+    # request stream through the server
+    reqs = [serving.c5_request(i, 1000 + i) for i in range(24)]
+    srv = serving.Server(96 << 30, lanes=4, max_batch=8, precision='mixed')
+    st = serving.run_stream(reqs, rate_hz=20.0, server=srv)
+    st.update({'arrivals': 'Poisson 20/s', 'lanes': 4, 'hbm_budget_bytes': 96 << 30})
+    out['serving_stream_mixed'] = st
+    return out
+
+
 def run_reference(args, rank, world):
     """The reference's algorithm on the host CPU (the oracle; the C++ reference needs
     Eigen and FFTW, absent here), same workload and metric."""
@@ -269,11 +344,10 @@ def main():
     lat_ms = [a.elapsed_time(b) for a, b in lat]
     cg_per_solve = (mixed.get_counter() - c0) / args.steps
     newton_mixed = r.nb_it
-    if pg:
-        t = torch.tensor([t_ms], device='cuda')
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        t_ms = float(t.item())
-    value = world * args.steps / (t_ms / 1000.0)
+    # replicas: every rank solves its own RVE; all solves over the slowest rank's time
+    from muspectre_gb300 import replicas
+    value, t_s, _ = replicas.aggregate_throughput(args.steps, t_ms / 1000.0)
+    t_ms = t_s * 1000.0
     stress_mixed = None
 
     # per-kernel profile of one CG iteration (mixed) + roofline
@@ -360,6 +434,8 @@ def main():
         'launch_shapes': cell.tuning(),
         'e2e': {'value': e2e_v, 'unit': 'solves/s', 'h2d_bytes_per_step': h2d, 'd2h_bytes_per_step': d2h},
     }
+    if rank == 0 and world == 1 and not args.no_extra:
+        line['configs'] = extra_configs(mu, workloads)
     if rank == 0 and not args.no_cpu:
         cb = cpu_baseline(w, r64.nb_it, int(round(fp64_cg_per_solve)), args.cpu_cg_iters)
         line['cpu_baseline'] = {'value': cb['solves_per_s'], 'unit': 'solves/s', 'cores': cb['cores'], 'kind': 'port',
