@@ -248,10 +248,10 @@ def extra_configs(mu, workloads):
         'note': 'the reference method (projector logm, j-independent Kirchhoff tangent) does not solve this '
                 'configuration; the oracle and the FP64 GPU path end the same way'}
     # request stream through the server
-    reqs = [serving.c5_request(i, 1000 + i) for i in range(24)]
+    reqs = [serving.c5_request(i, 1000 + i) for i in range(48)]
     srv = serving.Server(96 << 30, lanes=4, max_batch=8, precision='mixed')
-    st = serving.run_stream(reqs, rate_hz=20.0, server=srv)
-    st.update({'arrivals': 'Poisson 20/s', 'lanes': 4, 'hbm_budget_bytes': 96 << 30})
+    st = serving.run_stream(reqs, rate_hz=100.0, server=srv)
+    st.update({'arrivals': 'Poisson 100/s', 'lanes': 4, 'hbm_budget_bytes': 96 << 30})
     out['serving_stream_mixed'] = st
     return out
 
