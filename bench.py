@@ -153,6 +153,16 @@ def algorithmic_bytes(name, npx, nk, d2, s, tm):
     }.get(name, 0)
 
 
+def measured_traffic(kernel, n):
+    """DRAM bytes (read + write) per launch of a CG-iteration kernel from the committed
+    ncu capture of this workload (profiles/dram_spheres128_mixed.md), or None."""
+    path = os.path.join(ROOT, 'profiles', 'traffic_spheres128_mixed.json')
+    if n != 128 or not os.path.exists(path):
+        return None
+    with open(path) as f:
+        return json.load(f)['bytes_per_launch'].get(kernel)
+
+
 def cpu_baseline(w, newton_steps, cg_iters, nit):
     """Oracle (NumPy/SciPy, FP64) on a bounded sample of the workload: one material
     evaluation and `nit` CG iterations at full size, scaled to one solve by the FP64
@@ -363,7 +373,7 @@ def main():
     tot = sum(v['ms'] for v in kern.values())
     dom = max(kern, key=lambda k: kern[k]['ms'])
     roof = {'bound': 'hbm', 'kernel': dom, 'achieved': kern[dom]['gbs'], 'peak': peak, 'unit': 'GB/s',
-            'frac': (kern[dom]['gbs'] / peak) if kern[dom]['gbs'] else None, 'traffic': None,
+            'frac': (kern[dom]['gbs'] / peak) if kern[dom]['gbs'] else None, 'traffic': measured_traffic(dom, args.n),
             'peak_source': peak_kind, 'share': kern[dom]['ms'] / tot if tot else None,
             'iteration_ms': tot,
             'iteration_gbs': sum(v['bytes'] for v in kern.values()) / (tot * 1e-3) / 1e9 if tot else None,
