@@ -173,7 +173,8 @@ int musg_solver_cg_create(musg_cell *cell, double tol, unsigned maxiter,
                           int verbose, int precision, musg_solver **out);
 int musg_solver_destroy(musg_solver *solver);
 /* MUSG_PRECISION_MIXED only (no counterpart in the reference): the FP32 inner
- * solve stops at max(tol, inner_tol), default 1e-5, and newton_cg refines in FP64 */
+ * solve stops at max(tol, inner_tol), default 1e-2 (the forcing term of an inexact
+ * Newton method), and newton_cg refines in FP64 */
 int musg_solver_set_inner_tol(musg_solver *solver, double inner_tol);
 /* SolverBase::get_counter / reset_counter / has_converged (solver_base.hh:62-109) */
 int musg_solver_get_counter(musg_solver *solver, unsigned *counter);

@@ -18,7 +18,7 @@ from .solvers import OptimizeResult
 
 
 class BatchSolver:
-    def __init__(self, cells, tol, maxiter, precision='fp64', inner_tol=1e-5):
+    def __init__(self, cells, tol, maxiter, precision='fp64', inner_tol=1e-2):
         if precision not in ('fp64', 'mixed'):
             raise ValueError("precision must be 'fp64' or 'mixed'")
         self.cells = list(cells)

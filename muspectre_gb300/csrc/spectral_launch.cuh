@@ -5,6 +5,7 @@
 #include <algorithm>
 #include <mutex>
 #include <set>
+#include <vector>
 
 #include "spectral.cuh"
 #include "spectral_reg.cuh"
@@ -545,10 +546,19 @@ template <typename R> void spectral_autotune(Spectral &sp, cudaStream_t s, int e
       float best = 1e30f;
       int bt = sp.tune_threads[pi][pass];
       long bb = sp.tune_bytes[pi][pass];
-      // the register-resident passes take their block shape from the tile alone
+      // the register-resident passes take their block shape from the tile alone:
+      // sweep tiles of T pencils directly (the shared-memory target of T pencils)
       const bool reg = (pass == 1 && reg_axis(sp.ax[1])) || (pass == 2 && reg_axis(sp.ax[0]) && gm != GM_FWD);
+      std::vector<long> cand(bytes, bytes + sizeof(bytes) / sizeof(bytes[0]));
+      if (reg) {
+        const int m = sp.ax[pass == 1 ? 1 : 0].m;
+        const long nc = pass == 1 ? 1 : (gm == GM_FINITE ? sp.g.dim : (long)sp.g.dim * sp.g.dim);
+        const long pencil = nc * m * (long)sizeof(typename V2<R>::T);
+        cand.clear();
+        for (long T : {4L, 8L, 12L, 16L, 24L, 32L}) cand.push_back(T * pencil);
+      }
       for (int th : threads)
-        for (long by : bytes) {
+        for (long by : cand) {
           if (reg && th != threads[0]) continue;
           sp.tune_threads[pi][pass] = th;
           sp.tune_bytes[pi][pass] = by;

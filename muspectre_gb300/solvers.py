@@ -4,9 +4,11 @@
 ``precision='mixed'`` runs the CG, FFTs, projection and tangent in FP32 with
 compensated dot products while the Newton level (residual, increments, stress,
 return mapping) stays FP64.  The FP32 inner solve stops at max(tol, inner_tol)
-(default 1e-5: FP32 CG stalls and then diverges below ~1e-6 on stiff-contrast
-cells) and the FP64 Newton loop refines; for history-free materials the returned
-stress is evaluated at the returned strain.  ``newton_cg`` follows
+(default 1e-2, the forcing term of an inexact Newton method: each Newton step
+contracts the error by about inner_tol and the FP64 Newton loop refines to
+newton_tol, which takes fewer CG iterations in total than tight inner solves) and
+the FP64 Newton loop refines; for history-free materials the returned stress is
+evaluated at the returned strain.  ``newton_cg`` follows
 src/solver/solvers.cc:44-217.
 """
 from __future__ import annotations
@@ -39,7 +41,7 @@ class SolverBase:
 class SolverCG(SolverBase):
     """SolverCG (src/solver/solver_cg.hh:51-106, solver_cg.cc:54-110)."""
 
-    def __init__(self, cell, tol, maxiter, verbose=False, precision='fp64', inner_tol=1e-5):
+    def __init__(self, cell, tol, maxiter, verbose=False, precision='fp64', inner_tol=1e-2):
         if precision not in ('fp64', 'mixed'):
             raise ValueError("precision must be 'fp64' or 'mixed'")
         self.cell = cell
