@@ -56,6 +56,8 @@ extern "C" {
 #define MUSG_LAW_LE3 3  /* MaterialLinearElastic3:  per pixel (E, nu), full C   */
 #define MUSG_LAW_LE4 4  /* MaterialLinearElastic4:  per pixel (E, nu) -> (lambda, mu) */
 #define MUSG_LAW_HEP1 5 /* MaterialHyperElastoPlastic1: params (E, nu, tau_y0, H) */
+#define MUSG_LAW_GENERIC 6 /* MaterialLinearElasticGeneric: params the Voigt stiffness,
+                              vsize x vsize row-major (vsize 3 in 2-D, 6 in 3-D) */
 
 /* projection kinds */
 #define MUSG_PROJ_SMALL_STRAIN 0       /* ProjectionSmallStrain       */

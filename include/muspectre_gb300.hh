@@ -6,6 +6,7 @@
  *   make_cell<Dim>(res, lengths, form) / CellBase<Dim>      cell_factory.hh:93-105, cell_base.hh:70-526
  *   MaterialLinearElastic{1,2,3,4}<Dim>::make(cell, ...)    material_muSpectre_base.hh:135-137
  *   MaterialHyperElastoPlastic1<Dim>::make(cell, ...)       material_hyper_elasto_plastic1.hh
+ *   MaterialLinearElasticGeneric<Dim>::make(cell, name, C_voigt)  material_linear_elastic_generic.hh
  *   SolverCG(cell, tol, maxiter, verbose)                   solver_cg.hh, solver_base.hh:62-109
  *   newton_cg(cell, load_steps, solver, newton_tol, equil_tol, verbose)  solvers.hh:54-74
  *   FFTEngine, ProjectionSmallStrain / ProjectionFiniteStrain(Fast)       fft_engine_base.hh, projection_*.hh
@@ -312,6 +313,20 @@ template <int Dim, int LAW> class MaterialLinearElasticPerPixel : public Materia
 };
 template <int Dim> using MaterialLinearElastic3 = MaterialLinearElasticPerPixel<Dim, MUSG_LAW_LE3>;
 template <int Dim> using MaterialLinearElastic4 = MaterialLinearElasticPerPixel<Dim, MUSG_LAW_LE4>;
+
+// MaterialLinearElasticGeneric (material_linear_elastic_generic.cc:40-66): a constant
+// stiffness tensor from a Voigt matrix, vsize x vsize row-major (vsize 3 in 2-D, 6 in 3-D)
+template <int Dim> class MaterialLinearElasticGeneric : public MaterialBase {
+ public:
+  MaterialLinearElasticGeneric(Cell &c, const std::string &name, const std::vector<Real> &C_voigt)
+      : MaterialBase(c, MUSG_LAW_GENERIC, name, C_voigt) {}
+  static MaterialLinearElasticGeneric &make(CellBase<Dim> &cell, const std::string &name,
+                                           const std::vector<Real> &C_voigt) {
+    return cell.adopt(std::make_unique<MaterialLinearElasticGeneric>(cell, name, C_voigt));
+  }
+  void add_pixel(const std::array<int, Dim> &c) { add({index_of(c.data())}, {}, 0); }
+  void add_pixels(const std::vector<long long> &idx) { add(idx, {}, 0); }
+};
 
 // MaterialHyperElastoPlastic1 (material_hyper_elasto_plastic1.cc:41-65)
 template <int Dim> class MaterialHyperElastoPlastic1 : public MaterialBase {

@@ -19,7 +19,7 @@ OK, ERR_RUNTIME, ERR_PROJECTION, ERR_SOLVER, ERR_CONVERGENCE, ERR_SHAPE, ERR_CUD
 FINITE_STRAIN, SMALL_STRAIN = 0, 1
 FLAG_ALLOW_EVEN = 1
 PRECISION_FP64, PRECISION_MIXED = 0, 1
-LAW_LE1, LAW_LE2, LAW_LE3, LAW_LE4, LAW_HEP1 = 1, 2, 3, 4, 5
+LAW_LE1, LAW_LE2, LAW_LE3, LAW_LE4, LAW_HEP1, LAW_GENERIC = 1, 2, 3, 4, 5, 6
 PROJ_SMALL_STRAIN, PROJ_FINITE_STRAIN_FAST, PROJ_FINITE_STRAIN = 0, 1, 2
 
 

@@ -113,7 +113,36 @@ struct Material {
   std::vector<long long> pixels;
   std::vector<double> per_pixel;  // stride values per pixel
   int stride = 0;
+  std::vector<double> C;          // MaterialLinearElasticGeneric: D^4 stiffness (T4 layout)
 };
+
+// MaterialLinearElasticGeneric (material_linear_elastic_generic.cc:40-66): C(i,j,k,l) =
+// C_voigt(sym(i,j), sym(k,l)) with the Voigt index map of voigt_conversion.hh:118-125
+std::vector<double> stiffness_from_voigt(const double *voigt, int dim) {
+  static const int sym2[2][2] = {{0, 2}, {2, 1}};
+  static const int sym3[3][3] = {{0, 5, 4}, {5, 1, 3}, {4, 3, 2}};
+  const int vs = dim == 2 ? 3 : 6, D2 = dim * dim;
+  auto sym = [&](int i, int j) { return dim == 2 ? sym2[i][j] : sym3[i][j]; };
+  std::vector<double> C((size_t)D2 * D2);
+  for (int l = 0; l < dim; ++l)
+    for (int k = 0; k < dim; ++k)
+      for (int j = 0; j < dim; ++j)
+        for (int i = 0; i < dim; ++i) C[(i + dim * j) + D2 * (k + dim * l)] = voigt[sym(i, j) * vs + sym(k, l)];
+  return C;
+}
+
+// isotropic C = lam I (x) I + mu (I_sym doubled) (materials_toolbox.hh:638-652)
+std::vector<double> stiffness_isotropic(double lam, double mu, int dim) {
+  const int D2 = dim * dim;
+  std::vector<double> C((size_t)D2 * D2);
+  for (int l = 0; l < dim; ++l)
+    for (int k = 0; k < dim; ++k)
+      for (int j = 0; j < dim; ++j)
+        for (int i = 0; i < dim; ++i)
+          C[(i + dim * j) + D2 * (k + dim * l)] =
+              (i == j && k == l ? lam : 0.0) + mu * ((i == k && j == l ? 1.0 : 0.0) + (i == l && j == k ? 1.0 : 0.0));
+  return C;
+}
 
 }  // namespace
 
@@ -138,7 +167,8 @@ struct musg_cell {
   bool has_le2 = false, has_hep = false;
   // device fields (FP64 component planes)
   DevBuf F, P, rhs, io, io2;
-  DevBuf mat, params, law_kind;
+  DevBuf mat, params, law_kind, Ctab64, Ctab32;
+  bool has_generic = false;
   DevBuf lam64, mu64, lam32, mu32, eig;
   DevBuf Fprev[2], be[2], eps[2];
   DevBuf S64, S32, Kp64, Kp32, Fc64, Fc32, Kfull;
@@ -254,6 +284,7 @@ struct musg_cell {
         any_le = true;
       }
       if (mt.law == MUSG_LAW_LE2) has_le2 = true;
+      if (mt.law == MUSG_LAW_GENERIC) has_generic = true;
       for (size_t k = 0; k < mt.pixels.size(); ++k) {
         const long long p = mt.pixels[k];
         hmat[p] = (uint8_t)m;
@@ -273,6 +304,25 @@ struct musg_cell {
     else if (has_hep && any_le) tkind = TK_MIXED;
     else if (has_hep) tkind = TK_KPRIME;
     else tkind = TK_FINITE;
+    if (has_generic) {
+      // per-material stiffness tables: every material of the cell has a constant C
+      for (const Material &mt : materials)
+        require(mt.law == MUSG_LAW_LE1 || mt.law == MUSG_LAW_LE2 || mt.law == MUSG_LAW_GENERIC, MUSG_ERR_ARGUMENT,
+                "MaterialLinearElasticGeneric shares a cell with LE1, LE2 and generic materials only");
+      tkind = form == MUSG_SMALL_STRAIN ? TK_GSMALL : TK_GFINITE;
+      std::vector<double> ct;
+      for (size_t m = 0; m < materials.size(); ++m) {
+        const std::vector<double> Cm = materials[m].law == MUSG_LAW_GENERIC
+                                           ? materials[m].C
+                                           : stiffness_isotropic(hp[m].lam, hp[m].mu, dim);
+        ct.insert(ct.end(), Cm.begin(), Cm.end());
+      }
+      std::vector<float> cf(ct.begin(), ct.end());
+      Ctab64.alloc(ct.size() * sizeof(double));
+      Ctab32.alloc(cf.size() * sizeof(float));
+      MUSG_CUDA(cudaMemcpy(Ctab64.p, ct.data(), Ctab64.bytes, cudaMemcpyHostToDevice));
+      MUSG_CUDA(cudaMemcpy(Ctab32.p, cf.data(), Ctab32.bytes, cudaMemcpyHostToDevice));
+    }
     // the FP32 operator rebuilds S from F where the law allows (not LE2: eigenstrain)
     tkind32 = (tkind == TK_FINITE && !has_le2) ? TK_FISO : tkind;
     mat.alloc(npx);
@@ -369,6 +419,7 @@ struct musg_cell {
     a.lam = lam64.as<double>();
     a.mu = mu64.as<double>();
     a.eig = has_le2 ? eig.as<double>() : nullptr;
+    a.Ctab = Ctab64.as<double>();
     for (int b = 0; b < 2; ++b) {
       a.Fprev[b] = Fprev[b].as<double>();
       a.be[b] = be[b].as<double>();
@@ -420,6 +471,7 @@ template <> TangentData<double> musg_cell::tangent<double>() const {
   t.Kp = Kp64.as<double>();
   t.mat = mat.as<uint8_t>();
   t.law_kind = law_kind.as<uint8_t>();
+  t.C = Ctab64.as<double>();
   return t;
 }
 
@@ -432,6 +484,7 @@ template <> TangentData<float> musg_cell::tangent<float>() const {
   t.Kp = Kp32.as<float>();
   t.mat = mat.as<uint8_t>();
   t.law_kind = law_kind.as<uint8_t>();
+  t.C = Ctab32.as<float>();
   return t;
 }
 
@@ -1101,6 +1154,17 @@ int musg_material_create(musg_cell *cell, int law, const char *name, const doubl
       case MUSG_LAW_LE4:
         m.stride = 2;
         break;
+      case MUSG_LAW_GENERIC: {
+        const int vs = cell->dim == 2 ? 3 : 6;
+        if (nb_params != vs * vs) {
+          std::ostringstream err;
+          err << "The stiffness tensor should be input as a " << vs << " × " << vs
+              << " Matrix in Voigt notation. You supplied " << nb_params << " values";
+          throw Error(MUSG_ERR_ARGUMENT, err.str());
+        }
+        m.C = stiffness_from_voigt(params, cell->dim);
+        break;
+      }
       case MUSG_LAW_HEP1:
         require(nb_params >= 4, MUSG_ERR_ARGUMENT, "this material needs (Young, Poisson, tau_y0, H)");
         m.E = params[0];

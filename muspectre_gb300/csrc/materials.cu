@@ -260,11 +260,24 @@ __global__ void __launch_bounds__(kMatThreads) k_material(const MaterialArgs a, 
     M<D> S;
     const double tr = trace<D>(E);
     const bool tens = (mp.law == MUSG_LAW_LE3 || mp.law == MUSG_LAW_LE4);
+    const bool generic = (mp.law == MUSG_LAW_GENERIC);
+    const double *C = generic ? a.Ctab + (size_t)a.mat[px] * (D2 * D2) : nullptr;
+    if (generic) {
+      // MaterialLinearElasticGeneric: S = C:E (tensmult, material_linear_elastic_generic.hh)
 #pragma unroll
-    for (int j = 0; j < D; ++j)
+      for (int c = 0; c < D2; ++c) {
+        double v = 0.0;
 #pragma unroll
-      for (int i = 0; i < D; ++i)
-        S(i, j) = (tens ? mu * (E(i, j) + E(j, i)) : 2.0 * mu * E(i, j)) + (i == j ? lam * tr : 0.0);
+        for (int q = 0; q < D2; ++q) v += C[c + D2 * q] * E.a[q];
+        S.a[c] = v;
+      }
+    } else {
+#pragma unroll
+      for (int j = 0; j < D; ++j)
+#pragma unroll
+        for (int i = 0; i < D; ++i)
+          S(i, j) = (tens ? mu * (E(i, j) + E(j, i)) : 2.0 * mu * E(i, j)) + (i == j ? lam * tr : 0.0);
+    }
     if (finite) {
       P = mul<D>(F, S);  // PK1 = F S (materials_toolbox.hh:313-322)
 #pragma unroll
@@ -286,7 +299,19 @@ __global__ void __launch_bounds__(kMatThreads) k_material(const MaterialArgs a, 
 #pragma unroll
             for (int i = 0; i < D; ++i) {
               double v;
-              if (finite) {
+              if (generic) {
+                // small strain: K = C; finite: K(i,j,k,l) = d_ik S(j,l) + sum_rs F(i,r) C(r,j,l,s) F(k,s)
+                // (materials_toolbox.hh:313-350)
+                if (finite) {
+                  v = (i == k ? S(j, l) : 0.0);
+#pragma unroll
+                  for (int r = 0; r < D; ++r)
+#pragma unroll
+                    for (int s2 = 0; s2 < D; ++s2) v += F(i, r) * C[(r + D * j) + D2 * (l + D * s2)] * F(k, s2);
+                } else {
+                  v = C[(i + D * j) + D2 * (k + D * l)];
+                }
+              } else if (finite) {
                 // K(i,j,k,l) = d_ik S(j,l) + lam F(i,j) F(k,l) + mu (F(i,l) F(k,j) + d_jl (F F^T)(i,k))
                 double ffT = 0.0;
 #pragma unroll

@@ -94,6 +94,8 @@ enum TangentKind : int {
   TK_KPRIME = 3,  // j-independent Kirchhoff tangent: dP(i,m) = sum_n K'(i,m,n) sum_j dF(j,n)
   TK_MIXED = 4,   // per-pixel choice between TK_FINITE and TK_KPRIME by material law
   TK_FISO = 5,    // TK_FINITE with S rebuilt from F per application (isotropic LE1/LE3/LE4)
+  TK_GSMALL = 6,  // small strain, per-material stiffness C (MaterialLinearElasticGeneric): dP = C:de
+  TK_GFINITE = 7, // finite strain, per-material C: dP = dF S + F (C:(F^T dF))
 };
 
 // Device data the CG operator reads (precision R).
@@ -105,6 +107,7 @@ template <typename R> struct TangentData {
   const R *Kp = nullptr;    // [D^3][npx]  (Kirchhoff tangent)
   const uint8_t *mat = nullptr;      // [npx] material index (TK_MIXED)
   const uint8_t *law_kind = nullptr; // [kMaxMaterials]: TK_FINITE or TK_KPRIME (TK_MIXED)
+  const R *C = nullptr;     // [nmat][D^4] stiffness per material (TK_GSMALL / TK_GFINITE)
 };
 
 // CG scalar state, resident on the device (all FP64).
@@ -244,6 +247,7 @@ struct MaterialArgs {
   const MatParams *params;  // [nmat]
   const double *lam, *mu;   // [npx] (elastic laws)
   const double *eig;        // [D*D][npx] eigenstrain (LE2), may be null
+  const double *Ctab;       // [nmat][D^4] stiffness of MaterialLinearElasticGeneric materials
   // HEP1 state, two buffers each; cur selects the current one
   double *Fprev[2], *be[2], *eps[2];
   int cur;

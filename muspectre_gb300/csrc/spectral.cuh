@@ -189,26 +189,71 @@ __device__ __forceinline__ void tangent_kprime(const R *dF, const R *Kp, R *out)
   }
 }
 
+// per-material stiffness C (T4 layout (i + D j) + D^2 (k + D l)), MaterialLinearElasticGeneric
+// (material_linear_elastic_generic.hh): small strain dP = C:de; finite strain
+// dP = dF S + F (C:(F^T dF)) (the PK2/Green-Lagrange law linearised,
+// materials_toolbox.hh:313-350 contracted with dF)
+template <int D, typename R>
+__device__ __forceinline__ void tangent_generic_small(const R *e, const R *__restrict__ C, R *out) {
+#pragma unroll
+  for (int c = 0; c < D * D; ++c) {
+    R v = R(0);
+#pragma unroll
+    for (int q = 0; q < D * D; ++q) v += __ldg(&C[c + D * D * q]) * e[q];
+    out[c] = v;
+  }
+}
+template <int D, typename R>
+__device__ __forceinline__ void tangent_generic_finite(const R *dF, const R *F, const R *S, const R *__restrict__ C,
+                                                       R *out) {
+  R A[D * D];
+#pragma unroll
+  for (int n = 0; n < D; ++n)
+#pragma unroll
+    for (int s = 0; s < D; ++s) {
+      R a = R(0);
+#pragma unroll
+      for (int j = 0; j < D; ++j) a += F[j + D * s] * dF[j + D * n];
+      A[s + D * n] = a;  // (F^T dF)(s, n)
+    }
+  R B[D * D];
+  tangent_generic_small<D, R>(A, C, B);
+#pragma unroll
+  for (int m = 0; m < D; ++m)
+#pragma unroll
+    for (int i = 0; i < D; ++i) {
+      R v = R(0);
+#pragma unroll
+      for (int n = 0; n < D; ++n) v += dF[i + D * n] * S[n + D * m];
+#pragma unroll
+      for (int r = 0; r < D; ++r) v += F[i + D * r] * B[r + D * m];
+      out[i + D * m] = v;
+    }
+}
+
 // Tangent data of one pixel, loaded into registers before anything is stored so that
 // all of a pixel's global loads are in flight together.
 template <int D, int TK, typename R> struct TangentLocal {
   static constexpr int D2 = D * D;
-  static constexpr bool kFinite = (TK == TK_FINITE || TK == TK_MIXED || TK == TK_FISO);
+  static constexpr bool kFinite = (TK == TK_FINITE || TK == TK_MIXED || TK == TK_FISO || TK == TK_GFINITE);
+  static constexpr bool kGeneric = (TK == TK_GSMALL || TK == TK_GFINITE);
   static constexpr bool kKprime = (TK == TK_KPRIME || TK == TK_MIXED);
   int kind;
   R lam, mu;
   R F[kFinite ? D2 : 1], S[kFinite ? D2 : 1];
   R Kp[kKprime ? D2 * D : 1];
+  const R *Cm = nullptr;
 
   __device__ __forceinline__ void load(const TangentData<R> &td, long long px, long long npx) {
     kind = TK;
     if constexpr (TK == TK_MIXED) kind = td.law_kind[td.mat[px]];
-    if constexpr (TK == TK_SMALL || kFinite) {
+    if constexpr (kGeneric) Cm = td.C + (size_t)td.mat[px] * (D2 * D2);
+    if constexpr (TK == TK_SMALL || (kFinite && !kGeneric)) {
       lam = td.lam[px];
       mu = td.mu[px];
     }
     if constexpr (kFinite) {
-      if (TK == TK_FINITE || TK == TK_FISO || kind == TK_FINITE) {
+      if (TK == TK_FINITE || TK == TK_FISO || TK == TK_GFINITE || kind == TK_FINITE) {
 #pragma unroll
         for (int c = 0; c < D2; ++c) F[c] = td.F[c * npx + px];
         if constexpr (TK != TK_FISO) {
@@ -262,6 +307,10 @@ template <int D, int TK, typename R> struct TangentLocal {
       tangent_small<D, R>(in, lam, mu, out);
     } else if constexpr (TK == TK_FINITE || TK == TK_FISO) {
       tangent_finite<D, R>(in, F, S, lam, mu, out);
+    } else if constexpr (TK == TK_GSMALL) {
+      tangent_generic_small<D, R>(in, Cm, out);
+    } else if constexpr (TK == TK_GFINITE) {
+      tangent_generic_finite<D, R>(in, F, S, Cm, out);
     } else if constexpr (TK == TK_KPRIME) {
       tangent_kprime<D, R>(in, Kp, out);
     } else {

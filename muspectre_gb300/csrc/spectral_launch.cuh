@@ -143,6 +143,7 @@ void dispatch_fwd(int dim, int tk, const LastArgs<R> &a, const Cfg &c, cudaStrea
   if (dim == DD && tk == TT) { launch_fwd<R, PRO, DD, TT>(a, c, s, B); return; }
   MUSG_FWD_CASE(2, TK_SMALL) MUSG_FWD_CASE(2, TK_FINITE) MUSG_FWD_CASE(2, TK_KPRIME) MUSG_FWD_CASE(2, TK_MIXED)
   MUSG_FWD_CASE(3, TK_SMALL) MUSG_FWD_CASE(3, TK_FINITE) MUSG_FWD_CASE(3, TK_KPRIME) MUSG_FWD_CASE(3, TK_MIXED)
+  MUSG_FWD_CASE(2, TK_GSMALL) MUSG_FWD_CASE(2, TK_GFINITE) MUSG_FWD_CASE(3, TK_GSMALL) MUSG_FWD_CASE(3, TK_GFINITE)
   if (sizeof(R) == 4) {
     MUSG_FWD_CASE(2, TK_FISO) MUSG_FWD_CASE(3, TK_FISO)
   }
@@ -279,6 +280,7 @@ int last_cg_reg(Spectral &sp, int tkind, LastArgs<R> a, int G, bool inv, cudaStr
   if (sp.g.dim == DD && tkind == TT) { launch_fwd_reg<DD, TT>(m, a, grid, block, smem, s); return blocks; }
       MUSG_FR(2, TK_SMALL) MUSG_FR(2, TK_FINITE) MUSG_FR(2, TK_KPRIME) MUSG_FR(2, TK_MIXED) MUSG_FR(2, TK_FISO)
       MUSG_FR(3, TK_SMALL) MUSG_FR(3, TK_FINITE) MUSG_FR(3, TK_KPRIME) MUSG_FR(3, TK_MIXED) MUSG_FR(3, TK_FISO)
+      MUSG_FR(2, TK_GSMALL) MUSG_FR(2, TK_GFINITE) MUSG_FR(3, TK_GSMALL) MUSG_FR(3, TK_GFINITE)
 #undef MUSG_FR
       throw Error(MUSG_ERR_ARGUMENT, "unsupported tangent kind");
     }

@@ -154,6 +154,21 @@ class _HEP1(_Material):
         self._add([self._index(pixel)])
 
 
+class _Generic(_Material):
+    law = L.LAW_GENERIC
+
+    @classmethod
+    def make(cls, cell, name, C_voigt):
+        """MaterialLinearElasticGeneric(name, C_voigt) (material_linear_elastic_generic.cc:40-66):
+        a constant stiffness tensor given as a Voigt matrix (3 × 3 in 2-D, 6 × 6 in 3-D,
+        order xx, yy, [zz,] then yz, xz, xy).  The reference exposes it in C++ only."""
+        C = np.asarray(C_voigt, dtype=np.float64)
+        return cls(cell, name, list(C.reshape(-1)))
+
+    def add_pixel(self, pixel):
+        self._add([self._index(pixel)])
+
+
 MaterialLinearElastic1_2d = type('MaterialLinearElastic1_2d', (_LE1,), {})
 MaterialLinearElastic1_3d = type('MaterialLinearElastic1_3d', (_LE1,), {})
 MaterialLinearElastic2_2d = type('MaterialLinearElastic2_2d', (_LE2,), {})
@@ -164,3 +179,5 @@ MaterialLinearElastic4_2d = type('MaterialLinearElastic4_2d', (_LE4,), {})
 MaterialLinearElastic4_3d = type('MaterialLinearElastic4_3d', (_LE4,), {})
 MaterialHyperElastoPlastic1_2d = type('MaterialHyperElastoPlastic1_2d', (_HEP1,), {})
 MaterialHyperElastoPlastic1_3d = type('MaterialHyperElastoPlastic1_3d', (_HEP1,), {})
+MaterialLinearElasticGeneric_2d = type('MaterialLinearElasticGeneric_2d', (_Generic,), {})
+MaterialLinearElasticGeneric_3d = type('MaterialLinearElasticGeneric_3d', (_Generic,), {})

@@ -324,6 +324,42 @@ class MaterialLinearElastic1(Material):
         return pk1_from_pk2(F, law(E), C)
 
 
+# Voigt index map of voigt_conversion.hh:118-125 (sym_mat)
+VOIGT_SYM = {2: np.array([[0, 2], [2, 1]]), 3: np.array([[0, 5, 4], [5, 1, 3], [4, 3, 2]])}
+
+
+def stiffness_from_voigt(C_voigt, dim):
+    """material_linear_elastic_generic.cc:40-66: C(i,j,k,l) = C_voigt(sym(i,j), sym(k,l))."""
+    Cv = np.asarray(C_voigt, dtype=float)
+    vs = 3 if dim == 2 else 6
+    if Cv.shape != (vs, vs):
+        raise RuntimeError("The stiffness tensor should be input as a %d × %d Matrix in Voigt notation. "
+                           "You supplied a %d × %d matrix" % (vs, vs, Cv.shape[0], Cv.shape[1]))
+    s = VOIGT_SYM[dim]
+    return Cv[s[:, :, None, None], s[None, None, :, :]]
+
+
+class MaterialLinearElasticGeneric(Material):
+    """material_linear_elastic_generic.{hh,cc}: GL strain / PK2 stress with a constant
+    stiffness tensor given in Voigt notation; S = C:E (tensmult), tangent C."""
+
+    law = 'generic'
+
+    def __init__(self, name, dim, C_voigt):
+        super().__init__(name, dim)
+        self.C = stiffness_from_voigt(C_voigt, dim)
+
+    def add_pixel(self, index):
+        self.pixels.append(int(index))
+
+    def evaluate(self, F, form):
+        n = F.shape[0]
+        C = np.broadcast_to(self.C, (n,) + self.C.shape).copy()
+        if form == SMALL_STRAIN:
+            return tensmult(C, F), C
+        return pk1_from_pk2(F, tensmult(C, green_lagrange(F)), C)
+
+
 class MaterialLinearElastic2(MaterialLinearElastic1):
     """material_linear_elastic2.{hh,cc}: LE1 applied to (E - E_eig), per-pixel
     eigenstrain (add_pixel .cc:57-64; law .hh:179-201)."""

@@ -305,3 +305,20 @@ def test_small_strain_rejects_asymmetric_load():
     cell, _ = _laminate_cell()
     with pytest.raises(o.SolverError):
         o.newton_cg(cell, np.array([[0, 1.], [0, 0]]), o.SolverCG(cell, 1e-8, 20), 1e-5, 1e-10, 0)
+
+
+
+@pytest.mark.parametrize('dim', [2, 3])
+def test_generic_stiffness_from_voigt(dim):
+    """test_material_linear_elastic_generic.cc (C_test): the Voigt matrix of an isotropic
+    law with lambda = 2, mu = 1.5 gives Hooke's C_T4."""
+    lam, mu = 2.0, 1.5
+    vs = 3 if dim == 2 else 6
+    Cv = np.zeros((vs, vs))
+    Cv[:dim, :dim] = lam
+    Cv[:dim, :dim] += 2 * mu * np.eye(dim)
+    Cv[dim:, dim:] += mu * np.eye(vs - dim)
+    mat = o.MaterialLinearElasticGeneric('material', dim, Cv)
+    assert np.linalg.norm(mat.C - o.hooke_C(lam, mu, dim)) < 1e-14
+    with pytest.raises(RuntimeError):
+        o.MaterialLinearElasticGeneric('bad', dim, np.zeros((vs + 1, vs)))
