@@ -163,33 +163,49 @@ def measured_traffic(kernel, n):
         return json.load(f)['bytes_per_launch'].get(kernel)
 
 
+class CpuSample:
+    """The oracle (NumPy/SciPy, FP64, all host cores for its FFTs) on the full-size
+    workload: the Newton-level work (one material evaluation and the residual
+    projection) timed once, then CG iterations timed on demand; a solve is scaled from
+    them by the FP64 method's Newton and CG counts."""
+
+    def __init__(self, w):
+        from oracle import muspectre_oracle as o
+        from muspectre_gb300 import workloads
+        self.o = o
+        o.FFT_WORKERS = os.cpu_count() or 1
+        self.cell = workloads.build_spheres_oracle(o, w)
+        self.res = w['res']
+        d = 3
+        F = np.broadcast_to(np.eye(d) + w['load'], (self.cell.n_px, d, d)).copy()
+        self.cell.F = o.t2_to_vec(F)
+        t0 = time.perf_counter()
+        P, _ = self.cell.evaluate_stress_tangent()
+        self.rhs = -self.cell.apply_projection(P)
+        self.t_newton = time.perf_counter() - t0
+
+    def cg_iteration_seconds(self, nit=1):
+        solver = self.o.SolverCG(self.cell, 0.0, nit)
+        t0 = time.perf_counter()
+        try:
+            solver.solve(self.rhs)
+        except self.o.ConvergenceError:
+            pass  # tol 0: runs exactly nit iterations
+        return (time.perf_counter() - t0) / max(nit, 1)
+
+    def describe(self, t_cg, newton_steps, cg_iters, nit):
+        t_solve = newton_steps * self.t_newton + cg_iters * t_cg
+        return {'solves_per_s': 1.0 / t_solve, 'pxit_per_s': self.cell.n_px / t_cg, 't_cg_iter_s': t_cg,
+                't_newton_step_s': self.t_newton, 'cores': self.o.FFT_WORKERS,
+                'sample': 'material evaluation + residual projection once and %d CG iteration(s) at %d^3 (FP64), '
+                          'scaled to %d Newton steps and %d CG iterations per solve'
+                          % (nit, self.res[0], newton_steps, cg_iters)}
+
+
 def cpu_baseline(w, newton_steps, cg_iters, nit):
-    """Oracle (NumPy/SciPy, FP64) on a bounded sample of the workload: one material
-    evaluation and `nit` CG iterations at full size, scaled to one solve by the FP64
-    method's Newton/CG counts."""
-    from oracle import muspectre_oracle as o
-    from muspectre_gb300 import workloads
-    o.FFT_WORKERS = os.cpu_count() or 1
-    cell = workloads.build_spheres_oracle(o, w)
-    d = 3
-    F = np.broadcast_to(np.eye(d) + w['load'], (cell.n_px, d, d)).copy()
-    cell.F = o.t2_to_vec(F)
-    t0 = time.perf_counter()
-    P, _ = cell.evaluate_stress_tangent()
-    rhs = -cell.apply_projection(P)
-    t_newton = time.perf_counter() - t0
-    solver = o.SolverCG(cell, 0.0, nit)
-    t0 = time.perf_counter()
-    try:
-        solver.solve(rhs)
-    except o.ConvergenceError:
-        pass  # tol 0: runs exactly nit iterations
-    t_cg = (time.perf_counter() - t0) / max(nit, 1)
-    t_solve = newton_steps * t_newton + cg_iters * t_cg
-    return {'solves_per_s': 1.0 / t_solve, 'pxit_per_s': cell.n_px / t_cg, 't_cg_iter_s': t_cg,
-            't_newton_step_s': t_newton, 'cores': o.FFT_WORKERS,
-            'sample': '1 material evaluation + rhs projection and %d CG iterations at %d^3 (FP64), scaled to '
-                      '%d Newton steps and %d CG iterations per solve' % (nit, w['res'][0], newton_steps, cg_iters)}
+    """One bounded CPU sample of the workload (see CpuSample)."""
+    smp = CpuSample(w)
+    return smp.describe(smp.cg_iteration_seconds(nit), newton_steps, cg_iters, nit)
 
 
 def extra_configs(mu, workloads):
@@ -275,10 +291,11 @@ def run_reference(args, rank, world):
     w = workloads.spheres(args.n)
     ns = REF_NEWTON_STEPS or 3
     nc = REF_CG_ITERS or 600
+    smp = CpuSample(w)  # the cell and one Newton-level evaluation, timed once
     vals = []
     info = None
     for step in range(args.warmup + args.steps):
-        info = cpu_baseline(w, ns, nc, max(1, args.cpu_cg_iters // 2))
+        info = smp.describe(smp.cg_iteration_seconds(1), ns, nc, 1)  # one step = one CG iteration sample
         if step >= args.warmup:
             vals.append(info['solves_per_s'])
     v = statistics.median(vals)

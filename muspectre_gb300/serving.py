@@ -217,7 +217,7 @@ def solve_alone(req, tol=1e-8, maxiter=2000, newton_tol=1e-6, precision='mixed')
 
 
 def c5_request(rid, seed, small=False):
-    """BASELINE config 5 request drawn from its own seed: 2-D (64..1024, 2/3/5-smooth)
+    """A request of the mixed serving stream, drawn from its own seed: 2-D (64..1024, 2/3/5-smooth)
     or 3-D (32..160, 2/3/5-smooth); small or finite strain; LE1/LE4, or HEP1 with 1-10
     load steps (finite strain only); 1-60 spheres; E ~ U[1e9, 300e9], nu ~ U[0.2, 0.4];
     symmetric macro strain entries ~ U[-0.02, 0.02].  ``small`` caps the sizes (tests)."""

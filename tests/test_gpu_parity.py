@@ -278,7 +278,7 @@ def _readme_pair(mu):
 
 
 def test_readme_case_fp64(mu):
-    """The README example (BASELINE config 1): F and P within 1e-10 relative, same
+    """The README example (51x51 small strain, hard disc): F and P within 1e-10 relative, same
     Newton and CG iteration counts as the oracle."""
     ocell, gcell = _readme_pair(mu)
     Del0 = np.array([[.0, .0], [0, .03]])
@@ -346,7 +346,7 @@ def _oracle_variants(build, D, tol, ntol):
     (25, o.FINITE_STRAIN, 'le1', 'uniaxial'),
 ])
 def test_newton_cg_3d_fp64(mu, n, form, law, load):
-    """Odd twins of BASELINE configs 2 and 3 (finite-strain LE1 spheres, small-strain
+    """Odd twins of the 128^3 and 256^3 workloads (finite-strain LE1 spheres, small-strain
     lognormal LE4) in FP64.  Criteria: the strain field and the homogenised strain
     to 1e-10; the same number of Newton steps; CG counts within 1%; the returned
     stress (evaluated before the last Newton increment, so it carries the CG
@@ -476,7 +476,7 @@ def test_autotuned_shapes_same_results(mu):
 
 @pytest.mark.parametrize('logm', ['projector', 'spectral'])
 def test_hep1_uniaxial_config_status(mu, logm):
-    """BASELINE config 4 restated at 15³ (two HEP1 phases on a periodic Voronoi,
+    """The 64^3 two-phase HEP1 workload restated at 15³ (two HEP1 phases on a periodic Voronoi,
     uniaxial F11 ramp).  The reference method does not solve it: with the projector
     logm (eigen_tools.hh:209-322) the uniform first step has repeated eigenvalues and
     gives NaN; with the spectral logm the CG diverges on the j-independent
