@@ -129,6 +129,7 @@ __device__ __forceinline__ double cg_update_body(R alpha, R *__restrict__ x, R *
 template <typename R>
 __global__ void k_cg_update(CGState *__restrict__ st, R *__restrict__ x, R *__restrict__ r,
                             const R *__restrict__ p, const R *__restrict__ Ap, long long n, double *partial) {
+  dep_wait();
   if (!st->active) return;
   const double bs = cg_update_body<R>(R(st->alpha), x, r, p, Ap, n);
   if (threadIdx.x == 0) partial[blockIdx.x] = bs;
@@ -151,13 +152,14 @@ template <typename R>
 void cg_update(CGState *st, R *x, R *r, const R *p, const R *Ap, long long n, double *partial, cudaStream_t s) {
   if (!(aligned16(x) && aligned16(r) && aligned16(p) && aligned16(Ap)))
     throw Error(MUSG_ERR_ARGUMENT, "CG vectors must be 16-byte aligned");
-  k_cg_update<R><<<update_blocks(n), kRedThreads, 0, s>>>(st, x, r, p, Ap, n, partial);
+  launch_pdl(k_cg_update<R>, dim3(update_blocks(n)), dim3(kRedThreads), 0, s, st, x, r, p, Ap, n, partial);
   MUSG_CHECK_LAUNCH();
 }
 
 // ------------------------------------------------------------------ batched
 template <typename R>
 __global__ void k_cg_update_b(const BatchVec<R> *tab, long long n) {
+  dep_wait();
   const BatchVec<R> q = tab[blockIdx.y];
   if (!q.st->active) return;
   const double bs = cg_update_body<R>(R(q.st->alpha), q.x, q.r, q.p, q.Ap, n);
@@ -166,7 +168,7 @@ __global__ void k_cg_update_b(const BatchVec<R> *tab, long long n) {
 }
 
 template <typename R> void cg_update_batch(const BatchVec<R> *tab, long long n, int B, cudaStream_t s) {
-  k_cg_update_b<R><<<dim3(update_blocks(n), B), kRedThreads, 0, s>>>(tab, n);
+  launch_pdl(k_cg_update_b<R>, dim3(update_blocks(n), B), dim3(kRedThreads), 0, s, tab, n);
   MUSG_CHECK_LAUNCH();
 }
 

@@ -9,6 +9,7 @@
 #include <functional>
 #include <stdexcept>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "../../include/musg.h"
@@ -19,6 +20,7 @@ struct Error : std::runtime_error {
   int code;
   Error(int c, const std::string &m) : std::runtime_error(m), code(c) {}
 };
+
 
 // Runs f, maps an exception to a status code and the calling thread's last-error
 // message (the C-ABI convention of every musg_* entry point)
@@ -41,6 +43,30 @@ extern std::atomic<unsigned long long> g_launches;
     ::musg::g_launches.fetch_add(1);        \
     MUSG_CUDA(cudaGetLastError());          \
   } while (0)
+
+// Programmatic dependent launch: a kernel launched with launch_pdl may be scheduled
+// while the previous kernel of its stream finishes (its launch overlaps that tail);
+// it calls dep_wait() before it reads anything, which returns once the previous grid
+// has completed and its memory is visible.  No kernel here triggers early, so the
+// previous grid's blocks have all exited before any block of the next one runs.
+#ifdef __CUDACC__
+__device__ __forceinline__ void dep_wait() { asm volatile("griddepcontrol.wait;\n" ::: "memory"); }
+
+template <typename... KArgs, typename... Args>
+void launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s, Args &&...args) {
+  cudaLaunchConfig_t cfg{};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  MUSG_CUDA(cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...));
+}
+#endif
 
 template <typename R> struct V2;
 template <> struct V2<float> { using T = float2; };

@@ -365,6 +365,7 @@ template <typename R> struct LastArgs {
 // prologues (0 for PRO_PLAIN).
 template <typename R, int PRO, int D, int TK>
 __global__ void __launch_bounds__(kPassThreads) k_last_fwd(const LastArgs<R> a0) {
+  dep_wait();
   using T = typename V2<R>::T;
   LastArgs<R> a = a0;
   a.bind();
@@ -466,6 +467,7 @@ __global__ void __launch_bounds__(kPassThreads) k_last_fwd(const LastArgs<R> a0)
 // and the block sums of p.Ap.
 template <typename R, int EPI, int D>
 __global__ void __launch_bounds__(kPassThreads) k_last_inv(const LastArgs<R> a0) {
+  dep_wait();
   using T = typename V2<R>::T;
   LastArgs<R> a = a0;
   a.bind();
@@ -556,6 +558,7 @@ template <typename R> struct AxisArgs {
 
 template <typename R, bool INV>
 __global__ void __launch_bounds__(kPassThreads) k_axis(const AxisArgs<R> a0) {
+  dep_wait();
   using T = typename V2<R>::T;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T *buf = reinterpret_cast<T *>(smem_raw);
@@ -674,6 +677,7 @@ template <typename R> struct GreenArgs {
 
 template <typename R, int MODE, int D>
 __global__ void __launch_bounds__(kPassThreads) k_green(const GreenArgs<R> a0) {
+  dep_wait();
   using T = typename V2<R>::T;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T *buf = reinterpret_cast<T *>(smem_raw);

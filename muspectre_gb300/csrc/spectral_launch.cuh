@@ -129,7 +129,7 @@ template <typename R, int PRO, int D, int TK>
 void launch_fwd(const LastArgs<R> &a, const Cfg &c, cudaStream_t s, int B = 1) {
   auto k = k_last_fwd<R, PRO, D, TK>;
   allow_smem(k);
-  k<<<dim3(c.blocks, B), c.threads, c.smem, s>>>(a);
+  launch_pdl(k, dim3(c.blocks, B), dim3(c.threads), c.smem, s, a);
   MUSG_CHECK_LAUNCH();
 }
 
@@ -155,7 +155,7 @@ template <typename R, int EPI, int D>
 void launch_inv(const LastArgs<R> &a, const Cfg &c, cudaStream_t s, int B = 1) {
   auto k = k_last_inv<R, EPI, D>;
   allow_smem(k);
-  k<<<dim3(c.blocks, B), c.threads, c.smem, s>>>(a);
+  launch_pdl(k, dim3(c.blocks, B), dim3(c.threads), c.smem, s, a);
   MUSG_CHECK_LAUNCH();
 }
 
@@ -180,7 +180,7 @@ void launch_axis_reg(int m, const AxisArgs<R> &a, dim3 grid, dim3 block, size_t 
   case M: {                           \
     auto k = k_axis_reg<R, M, INV>;   \
     allow_smem(k);                    \
-    k<<<grid, block, smem, s>>>(a);   \
+    launch_pdl(k, grid, block, smem, s, a);   \
     break;                            \
   }
   switch (m) {
@@ -197,7 +197,7 @@ void launch_green_reg(int m, const GreenArgs<R> &a, dim3 grid, dim3 block, size_
   case M: {                                  \
     auto k = k_green_reg<R, M, MODE, D>;     \
     allow_smem(k);                           \
-    k<<<grid, block, smem, s>>>(a);          \
+    launch_pdl(k, grid, block, smem, s, a);          \
     break;                                   \
   }
   switch (m) {
@@ -233,7 +233,7 @@ void launch_fwd_reg(int m, const LastArgs<float> &a, dim3 grid, dim3 block, size
   case M: {                                   \
     auto k = k_last_fwd_reg<M, D, TK>;        \
     allow_smem(k);                            \
-    k<<<grid, block, smem, s>>>(a);           \
+    launch_pdl(k, grid, block, smem, s, a);           \
     break;                                    \
   }
   switch (m) {
@@ -250,7 +250,7 @@ void launch_inv_reg(int m, const LastArgs<float> &a, dim3 grid, dim3 block, size
   case M: {                                   \
     auto k = k_last_inv_reg<M, D>;            \
     allow_smem(k);                            \
-    k<<<grid, block, smem, s>>>(a);           \
+    launch_pdl(k, grid, block, smem, s, a);           \
     break;                                    \
   }
   switch (m) {
@@ -332,11 +332,11 @@ void run_axis(Spectral &sp, bool inv, const CGState *st, cudaStream_t s, const P
   if (inv) {
     auto k = k_axis<R, true>;
     allow_smem(k);
-    k<<<dim3(c.blocks, B), c.threads, c.smem, s>>>(a);
+    launch_pdl(k, dim3(c.blocks, B), dim3(c.threads), c.smem, s, a);
   } else {
     auto k = k_axis<R, false>;
     allow_smem(k);
-    k<<<dim3(c.blocks, B), c.threads, c.smem, s>>>(a);
+    launch_pdl(k, dim3(c.blocks, B), dim3(c.threads), c.smem, s, a);
   }
   MUSG_CHECK_LAUNCH();
 }
@@ -388,7 +388,7 @@ void run_green(Spectral &sp, int mode, const CGState *st, cudaStream_t s, const 
   {                                                              \
     auto k = k_green<R, MODE, DD>;                               \
     allow_smem(k);                                               \
-    k<<<dim3(c.blocks, B), c.threads, c.smem, s>>>(a);        \
+    launch_pdl(k, dim3(c.blocks, B), dim3(c.threads), c.smem, s, a);        \
   }
   if (mode == GM_FWD) MUSG_GREEN(GM_FWD, 2)
   else if (mode == GM_INV) MUSG_GREEN(GM_INV, 2)

@@ -53,6 +53,7 @@ __device__ __forceinline__ T reg_tw(const T *__restrict__ tw, int idx) {
 // tile + ntiles * slab, blockIdx.z = problem of a batched launch
 template <typename R, int M, bool INV>
 __global__ void __launch_bounds__(512) k_axis_reg(const AxisArgs<R> a0) {
+  dep_wait();
   using T = typename V2<R>::T;
   using F = RegFft<M>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -126,6 +127,7 @@ __global__ void __launch_bounds__(512) k_axis_reg(const AxisArgs<R> a0) {
 // slot-major [slot][z][t], NC * T pencils of M entries.
 template <typename R, int M, int MODE, int D>
 __global__ void __launch_bounds__(384, 2) k_green_reg(const GreenArgs<R> a0) {
+  dep_wait();
   using T = typename V2<R>::T;
   using F = RegFft<M>;
   static_assert(MODE == GM_SMALL || MODE == GM_FINITE, "projection modes only");
@@ -246,6 +248,7 @@ template <int M> struct LastLayout {
 // v = K:p per pixel, spectrum of v.  FP32 only.
 template <int M, int D, int TK>
 __global__ void __launch_bounds__(512) k_last_fwd_reg(const LastArgs<float> a0) {
+  dep_wait();
   using R = float;
   using T = float2;
   using F = RegFft<M>;
@@ -332,6 +335,7 @@ __global__ void __launch_bounds__(512) k_last_fwd_reg(const LastArgs<float> a0) 
 // the transform so that they are in flight with the spectrum.  FP32 only.
 template <int M, int D>
 __global__ void __launch_bounds__(384, 2) k_last_inv_reg(const LastArgs<float> a0) {
+  dep_wait();
   using R = float;
   using T = float2;
   using F = RegFft<M>;
