@@ -202,7 +202,6 @@ int cg_operator(Spectral &sp, int tkind, const TangentData<R> &td, const CGState
 template <typename R>
 void tangent_operator(Spectral &sp, int tkind, const TangentData<R> &td, const R *in,
                       R *out, cudaStream_t s);
-int cg_operator_partials(const Spectral &sp);
 // batched CG operator over B same-shape problems (one launch per pass; problem b
 // is blockIdx.y); tab is a device array of B ProblemPtrs (spectral.cuh), whose host
 // image is ProblemPtrsHost

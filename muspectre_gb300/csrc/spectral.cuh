@@ -49,21 +49,32 @@ template <> struct Acc<double> {
   __device__ __forceinline__ double value() const { return s; }
 };
 
-// sum of v over the block (1-, 2- or 3-D, a whole number of warps), result valid in
-// the thread of linear index 0
+// sum of v over the block (1-, 2- or 3-D, any number of threads), result valid in
+// the thread of linear index 0.  A partial last warp shuffles among its existing lanes
+// only (lanes past the block's end do not exist, so the mask names just the others and
+// their values are never added); whole warps add in the same order as a full tree.
 __device__ __forceinline__ double block_sum(double v) {
   __shared__ double red[32];
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  const int nth = blockDim.x * blockDim.y * blockDim.z;
   const int tid = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
   const int w = tid >> 5, l = tid & 31;
+  const int nl = min(32, nth - (w << 5));
+  const unsigned mask = nl == 32 ? 0xffffffffu : ((1u << nl) - 1u);
+  for (int o = 16; o > 0; o >>= 1) {
+    const double t = __shfl_down_sync(mask, v, o);
+    if (l + o < nl) v += t;
+  }
   __syncthreads();
   if (l == 0) red[w] = v;
   __syncthreads();
   v = 0.0;
   if (w == 0) {
-    const int nw = (blockDim.x * blockDim.y * blockDim.z + 31) >> 5;
+    const int nw = (nth + 31) >> 5;
     v = (l < nw) ? red[l] : 0.0;
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    for (int o = 16; o > 0; o >>= 1) {
+      const double t = __shfl_down_sync(mask, v, o);
+      if (l + o < nl) v += t;
+    }
   }
   return v;
 }

@@ -211,20 +211,27 @@ void launch_green_reg(int m, const GreenArgs<R> &a, dim3 grid, dim3 block, size_
 // last-axis register kernels (FP32 CG passes): rows per block G = 2 G2 with the
 // block (Y lanes, ncomp G2 pencils) a whole number of warps and at most 384 threads;
 // G = 0 when the axis or the shape does not allow them
-template <typename R> int last_reg_rows(const Spectral &sp) {
+// Rows per block of the register last-axis passes (two rows share one complex
+// transform, so G is even; a block is Y lanes x ncomp components x G/2 row pairs).
+// Measured on 128^3 finite-strain cells (9 components, Y = 8): the forward pass is
+// fastest at 144 threads (77 us; 78-86 us at 72, 216, 288 threads, 92 us at 360) and
+// the inverse at 216 (70 us; 74 us at 288, 77 at 144, 91 at 72).  Small blocks keep
+// more of them resident between the stage barriers; the rule takes the most row
+// pairs whose block stays within those thread counts.  0 = no register path.
+template <typename R> int last_reg_rows(const Spectral &sp, bool inv) {
   if (sizeof(R) != 4) return 0;
   const AxisPlan &ap = sp.ax[sp.g.dim - 1];
   if (!reg_axis(ap)) return 0;
   const int m = ap.m, Y = reg_lanes(m), nc = sp.ncomp;
   const long ps = (long)(m + m / RegLanesR1(m));
   const long per_g2 = (long)nc * ps * (long)sizeof(typename V2<R>::T);
-  long g2 = std::max(1L, sp.tune_bytes[prec_index<R>()][0] / per_g2);
+  const long target = inv ? 224 : 160, bound = inv ? 384 : 512;  // launch bounds of the kernels
+  const long th1 = (long)Y * nc;
+  if (th1 > bound || per_g2 > optin_smem()) return 0;
+  long g2 = std::max(1L, target / th1);
   g2 = std::min<long>(g2, (sp.g.nrows + 1) / 2);
-  for (; g2 >= 1; --g2) {
-    const long th = (long)Y * nc * g2;
-    if (th <= 384 && th % 32 == 0 && g2 * per_g2 <= optin_smem()) return (int)(2 * g2);  // k_last_inv_reg bound
-  }
-  return 0;
+  g2 = std::min<long>(g2, optin_smem() / per_g2);
+  return (int)(2 * g2);
 }
 
 template <int D, int TK>
@@ -463,9 +470,10 @@ int cg_operator(Spectral &sp, int tkind, const TangentData<R> &td, const CGState
   auto mark = [&]() {
     if (ev) MUSG_CUDA(cudaEventRecord(ev[k++], s));
   };
-  const int greg = last_reg_rows<R>(sp);
+  const int gfwd = last_reg_rows<R>(sp, false), ginv = last_reg_rows<R>(sp, true);
+  const bool greg = gfwd && ginv;
   mark();
-  if (greg) last_cg_reg<R>(sp, tkind, a, greg, false, s, 1);
+  if (greg) last_cg_reg<R>(sp, tkind, a, gfwd, false, s, 1);
   else dispatch_fwd<R, PRO_CG>(sp.g.dim, tkind, a, c, s);
   mark();
   if (sp.g.dim == 3) {
@@ -479,7 +487,7 @@ int cg_operator(Spectral &sp, int tkind, const TangentData<R> &td, const CGState
     mark();
   }
   if (greg) {
-    const int nb = last_cg_reg<R>(sp, tkind, a, greg, true, s, 1);
+    const int nb = last_cg_reg<R>(sp, tkind, a, ginv, true, s, 1);
     mark();
     return nb;
   }
@@ -499,13 +507,14 @@ int cg_operator_batch(Spectral &sp, int tkind, const ProblemPtrs<R> *tab, int B,
   const Cfg c = last_cfg<R>(sp);
   LastArgs<R> a = last_args<R>(sp, c);
   a.batch = tab;
-  const int greg = last_reg_rows<R>(sp);
-  if (greg) last_cg_reg<R>(sp, tkind, a, greg, false, s, B);
+  const int gfwd = last_reg_rows<R>(sp, false), ginv = last_reg_rows<R>(sp, true);
+  const bool greg = gfwd && ginv;
+  if (greg) last_cg_reg<R>(sp, tkind, a, gfwd, false, s, B);
   else dispatch_fwd<R, PRO_CG>(sp.g.dim, tkind, a, c, s, B);
   if (sp.g.dim == 3) run_axis<R>(sp, false, nullptr, s, tab, B);
   run_green<R>(sp, gm, nullptr, s, tab, B);
   if (sp.g.dim == 3) run_axis<R>(sp, true, nullptr, s, tab, B);
-  if (greg) return last_cg_reg<R>(sp, tkind, a, greg, true, s, B);
+  if (greg) return last_cg_reg<R>(sp, tkind, a, ginv, true, s, B);
   if (sp.g.dim == 2) launch_inv<R, EPI_CG, 2>(a, c, s, B);
   else launch_inv<R, EPI_CG, 3>(a, c, s, B);
   return c.blocks;
