@@ -646,6 +646,15 @@ struct musg_solver {
       }
       if (!hst->active) break;
     }
+    if (precision == MUSG_PRECISION_MIXED) {
+      unsigned fault = 0;
+      MUSG_CUDA(cudaMemcpyAsync(&fault, wait_fault_word(), sizeof fault, cudaMemcpyDeviceToHost, s));
+      MUSG_CUDA(cudaStreamSynchronize(s));
+      if (fault) {
+        MUSG_CUDA(cudaMemsetAsync(wait_fault_word(), 0, sizeof fault, s));
+        throw Error(MUSG_ERR_RUNTIME, "a spectral pass timed out waiting for its tile copy (device state unreliable)");
+      }
+    }
     counter = hst->counter;
     if (hst->rdr < hst->tol2) {
       converged = true;

@@ -169,11 +169,20 @@ struct Spectral {
   // the defaults below or by spectral_autotune
   int tune_threads[2][3] = {{256, 256, 256}, {256, 256, 256}};
   long tune_bytes[2][3] = {{73728, 49152, 73728}, {73728, 49152, 73728}};
+  // TMA descriptor of the FP32 spectrum for the Green pass (an opaque CUtensorMap,
+  // encoded on first use for the tile width and mode below) and its persistent grid
+  unsigned char green_tmap[128] = {};
+  const void *green_tmap_spec = nullptr;
+  int green_tmap_T = 0, green_tmap_mode = -1, green_tmap_grid = 0;
   void init(int dim, const int *res, int ncomp, int proj_kind, const double *lengths,
             bool allow_even, bool want32);
   void ensure32();
   void release();
 };
+
+// Device word set by a kernel whose bounded wait on an asynchronous copy ran out
+// (spectral_tma.cuh); its device address, for a stream-ordered read by the host
+unsigned *wait_fault_word();
 
 // Launch configuration limits of the pass kernels
 constexpr int kPassThreads = 512;

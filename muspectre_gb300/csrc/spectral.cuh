@@ -617,6 +617,11 @@ __global__ void __launch_bounds__(kPassThreads) k_axis(const AxisArgs<R> a0) {
 }
 
 // ------------------------------------------------------------ Green operators
+// 1 / sqrt(n2): FP64 correctly rounded division of the square root (parity path);
+// FP32 the rsqrtf intrinsic (2 ulp, far inside the FP32 operator's rounding)
+__device__ __forceinline__ double inv_sqrt(double n2) { return 1.0 / sqrt(n2); }
+__device__ __forceinline__ float inv_sqrt(float n2) { return rsqrtf(n2); }
+
 // unit wave vector of k-point (xi0[e], xi1[k1], xi2[k2]); false where the operator
 // is zero (the zero mode, and every Nyquist index under the even-grid extension)
 template <int D, typename R>
@@ -625,7 +630,7 @@ __device__ __forceinline__ bool unit_xi(R *xi, int e, int k1, int k2, int nyq0, 
   R n2 = R(0);
 #pragma unroll
   for (int d = 0; d < D; ++d) n2 += xi[d] * xi[d];
-  const R inv = R(1) / sqrt(n2);
+  const R inv = inv_sqrt(n2);
 #pragma unroll
   for (int d = 0; d < D; ++d) xi[d] *= inv;
   return true;

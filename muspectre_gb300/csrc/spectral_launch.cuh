@@ -12,6 +12,11 @@
 
 namespace musg {
 
+// The FP32 Green pass through the TMA-fed persistent kernel (spectral_tma.cu) for a
+// tile of Tt pencils; false (nothing launched) when the spectrum, the tile or the
+// driver does not qualify, and the caller launches the register kernel instead.
+bool launch_green_tma(Spectral &sp, int mode, const GreenArgs<float> &a, int Tt, cudaStream_t s);
+
 namespace {
 
 int optin_smem() {
@@ -382,6 +387,9 @@ void run_green(Spectral &sp, int mode, const CGState *st, cudaStream_t s, const 
     if (tmax >= 1) {
       const long Tt = reg_tile(sp.tune_bytes[prec_index<R>()][2], (long)nc * m * sizeof(T), tmax, Rr);
       a.T = (int)Tt;
+      if constexpr (sizeof(R) == 4) {
+        if (!batch && B == 1 && launch_green_tma(sp, mode, a, (int)Tt, s)) return;
+      }
       const dim3 grid((unsigned)((Rr + Tt - 1) / Tt), mode == GM_FINITE ? dim : 1, B), block((unsigned)Tt, Y, nc);
       const size_t smem = (size_t)nc * Tt * m * sizeof(T);
       if (mode == GM_FINITE && dim == 2) launch_green_reg<R, GM_FINITE, 2>(m, a, grid, block, smem, s);
