@@ -332,7 +332,8 @@ __global__ void __launch_bounds__(512) k_last_fwd_reg(const LastArgs<float> a0) 
 
 // inverse with the CG epilogue: Ap = real rows of the spectrum, partial[block] = sum
 // of p.Ap over the block's rows.  The p entries of a lane's outputs are loaded before
-// the transform so that they are in flight with the spectrum.  FP32 only.
+// the transform, after its spectrum entries, so that they are in flight with the
+// transform.  FP32 only.
 template <int M, int D>
 __global__ void __launch_bounds__(384, 2) k_last_inv_reg(const LastArgs<float> a0) {
   dep_wait();
@@ -353,18 +354,14 @@ __global__ void __launch_bounds__(384, 2) k_last_inv_reg(const LastArgs<float> a
   const long long rx = row0 + 2 * g2, ry = rx + 1;
   const bool okx = rx < a.nrows, oky = ry < a.nrows;
   const long long ox = (long long)c * a.npx + rx * L, oy = ox + L;
-  R px[F::R1], py[F::R1];
-#pragma unroll
-  for (int r = 0; r < F::R1; ++r) {
-    px[r] = okx ? a.p[ox + y + F::Y * r] : R(0);
-    py[r] = oky ? a.p[oy + y + F::Y * r] : R(0);
-  }
   const T *sx = a.spec + (long long)c * a.nk + rx * H;
   T *col = buf + q * Lay::PS;
+  // every spectrum entry of the lane first (the transform needs them), then p (the
+  // epilogue needs it), so the spectrum loads are not queued behind the p loads
+  T w[F::NB][F::R2];
 #pragma unroll
   for (int b = 0; b < F::NB; ++b) {
     const int j = y + F::Y * b;
-    T w[F::R2];
 #pragma unroll
     for (int r = 0; r < F::R2; ++r) {
       const int k = j + F::R1 * r;
@@ -380,13 +377,23 @@ __global__ void __launch_bounds__(384, 2) k_last_inv_reg(const LastArgs<float> a
         x.y = R(0);
         z.y = R(0);
       }
-      w[r] = T{x.x - z.y, x.y + z.x};
+      w[b][r] = T{x.x - z.y, x.y + z.x};
     }
-    Dft<F::R2, true, T>::run(w);
+  }
+  R px[F::R1], py[F::R1];
 #pragma unroll
-    for (int r = 1; r < F::R2; ++r) w[r] = cmul(w[r], reg_tw<true>(a.ap.tw, j * r));
+  for (int r = 0; r < F::R1; ++r) {
+    px[r] = okx ? a.p[ox + y + F::Y * r] : R(0);
+    py[r] = oky ? a.p[oy + y + F::Y * r] : R(0);
+  }
 #pragma unroll
-    for (int r = 0; r < F::R2; ++r) col[Lay::pos(j + F::R1 * r)] = w[r];
+  for (int b = 0; b < F::NB; ++b) {
+    const int j = y + F::Y * b;
+    Dft<F::R2, true, T>::run(w[b]);
+#pragma unroll
+    for (int r = 1; r < F::R2; ++r) w[b][r] = cmul(w[b][r], reg_tw<true>(a.ap.tw, j * r));
+#pragma unroll
+    for (int r = 0; r < F::R2; ++r) col[Lay::pos(j + F::R1 * r)] = w[b][r];
   }
   __syncthreads();
   T v[F::R1];
