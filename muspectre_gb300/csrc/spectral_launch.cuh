@@ -16,6 +16,10 @@ namespace musg {
 // tile of Tt pencils; false (nothing launched) when the spectrum, the tile or the
 // driver does not qualify, and the caller launches the register kernel instead.
 bool launch_green_tma(Spectral &sp, int mode, const GreenArgs<float> &a, int Tt, cudaStream_t s);
+// The FP32 last-axis inverse with the CG epilogue through the bulk-copy-fed
+// persistent kernel (spectral_tma.cu) for tiles of G rows; returns its number of
+// blocks (= partial sums), or 0 (nothing launched) when the shape does not qualify.
+int launch_last_inv_tma(Spectral &sp, const LastArgs<float> &a, int G, cudaStream_t s);
 
 namespace {
 
@@ -173,7 +177,7 @@ bool reg_axis(const AxisPlan &p) { return !p.blu && p.m == p.n && reg_fft_length
 // the inner extent
 long reg_tile(long target, long per_pencil, long tmax, long long inner) {
   long T = std::max(1L, std::min(tmax, target / per_pencil));
-  T = std::min<long>(T, (long)optin_smem() / per_pencil);
+  T = std::min<long>(T, (long)optin_smem() / per_pencil - 1);  // room for the twiddle table
   T = std::max(1L, std::min<long>(T, inner));
   const long nt = (long)((inner + T - 1) / T);
   return (long)((inner + nt - 1) / nt);
@@ -232,10 +236,10 @@ template <typename R> int last_reg_rows(const Spectral &sp, bool inv) {
   const long per_g2 = (long)nc * ps * (long)sizeof(typename V2<R>::T);
   const long target = inv ? 224 : 160, bound = inv ? 384 : 512;  // launch bounds of the kernels
   const long th1 = (long)Y * nc;
-  if (th1 > bound || per_g2 > optin_smem()) return 0;
+  if (th1 > bound || per_g2 + (long)m * (long)sizeof(float2) > optin_smem()) return 0;
   long g2 = std::max(1L, target / th1);
   g2 = std::min<long>(g2, (sp.g.nrows + 1) / 2);
-  g2 = std::min<long>(g2, optin_smem() / per_g2);
+  g2 = std::min<long>(g2, (optin_smem() - (long)m * (long)sizeof(float2)) / per_g2);  // + twiddle table
   return (int)(2 * g2);
 }
 
@@ -286,7 +290,7 @@ int last_cg_reg(Spectral &sp, int tkind, LastArgs<R> a, int G, bool inv, cudaStr
     const long ps = m + m / RegLanesR1(m);
     a.G = G;
     const dim3 grid(blocks, B), block(Y, nc * G2);
-    const size_t smem = (size_t)nc * G2 * ps * sizeof(float2);
+    const size_t smem = ((size_t)nc * G2 * ps + m) * sizeof(float2);  // pencils + twiddle table
     if (!inv) {
 #define MUSG_FR(DD, TT) \
   if (sp.g.dim == DD && tkind == TT) { launch_fwd_reg<DD, TT>(m, a, grid, block, smem, s); return blocks; }
@@ -295,6 +299,10 @@ int last_cg_reg(Spectral &sp, int tkind, LastArgs<R> a, int G, bool inv, cudaStr
       MUSG_FR(2, TK_GSMALL) MUSG_FR(2, TK_GFINITE) MUSG_FR(3, TK_GSMALL) MUSG_FR(3, TK_GFINITE)
 #undef MUSG_FR
       throw Error(MUSG_ERR_ARGUMENT, "unsupported tangent kind");
+    }
+    if (B == 1 && !a.batch) {
+      const int nb = launch_last_inv_tma(sp, a, G, s);
+      if (nb) return nb;
     }
     if (sp.g.dim == 2) launch_inv_reg<2>(m, a, grid, block, smem, s);
     else launch_inv_reg<3>(m, a, grid, block, smem, s);
@@ -324,7 +332,7 @@ void run_axis(Spectral &sp, bool inv, const CGState *st, cudaStream_t s, const P
     a.st = st;
     a.batch = batch;
     const dim3 grid((unsigned)(a.ntiles * nbatch), 1, B), block((unsigned)Tt, Y, 1);
-    const size_t smem = (size_t)Tt * m * sizeof(T);
+    const size_t smem = (size_t)(Tt + 1) * m * sizeof(T);  // tile + twiddle table
     if (inv) launch_axis_reg<R, true>(m, a, grid, block, smem, s);
     else launch_axis_reg<R, false>(m, a, grid, block, smem, s);
     return;
@@ -391,7 +399,7 @@ void run_green(Spectral &sp, int mode, const CGState *st, cudaStream_t s, const 
         if (!batch && B == 1 && launch_green_tma(sp, mode, a, (int)Tt, s)) return;
       }
       const dim3 grid((unsigned)((Rr + Tt - 1) / Tt), mode == GM_FINITE ? dim : 1, B), block((unsigned)Tt, Y, nc);
-      const size_t smem = (size_t)nc * Tt * m * sizeof(T);
+      const size_t smem = (size_t)(nc * Tt + 1) * m * sizeof(T);  // tile + twiddle table
       if (mode == GM_FINITE && dim == 2) launch_green_reg<R, GM_FINITE, 2>(m, a, grid, block, smem, s);
       else if (mode == GM_FINITE) launch_green_reg<R, GM_FINITE, 3>(m, a, grid, block, smem, s);
       else if (dim == 2) launch_green_reg<R, GM_SMALL, 2>(m, a, grid, block, smem, s);

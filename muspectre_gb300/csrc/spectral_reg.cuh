@@ -40,12 +40,24 @@ template <int M> struct RegFft {
 
 inline bool reg_fft_length(int m) { return m == 16 || m == 32 || m == 64 || m == 128 || m == 256; }
 
-// stage-2 twiddle W_M^(j r) (j < R1, r < R2, so j r < M) from the plan's table
+// stage-2 twiddle W_M^(j r) (j < R1, r < R2, so j r < M) from the block's shared
+// copy of the plan's table (stage_twiddles)
 template <bool CONJ, typename T>
-__device__ __forceinline__ T reg_tw(const T *__restrict__ tw, int idx) {
-  T w = __ldg(&tw[idx]);
+__device__ __forceinline__ T reg_tw(const T *tw, int idx) {
+  T w = tw[idx];
   if (CONJ) w.y = -w.y;
   return w;
+}
+
+// copy the plan's twiddle table W_M^k (k < M) into shared memory, by the whole block;
+// a barrier must separate it from the first reg_tw.  Per-thread loads of the table
+// from global memory (L1 hits) made the stage-2 butterflies wait on the load pipe:
+// the last-axis inverse ran 63.5 us with them and 49.2 us with the shared copy.
+template <int M, typename T>
+__device__ __forceinline__ void stage_twiddles(T *dst, const T *__restrict__ src) {
+  for (int k = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z); k < M;
+       k += blockDim.x * blockDim.y * blockDim.z)
+    dst[k] = src[k];
 }
 
 // ------------------------------------------------------------ middle-axis pass
@@ -65,6 +77,8 @@ __global__ void __launch_bounds__(512) k_axis_reg(const AxisArgs<R> a0) {
   }
   if (a.st && !a.st->active) return;
   const int Tt = blockDim.x, t = threadIdx.x, y = threadIdx.y;
+  T *tws = buf + (size_t)Tt * M;  // after the tile
+  stage_twiddles<M>(tws, a.ap.tw);
   const int tile = blockIdx.x % a.ntiles;
   const long long slab = blockIdx.x / a.ntiles;
   const long long pos = (long long)tile * Tt + t;
@@ -86,7 +100,7 @@ __global__ void __launch_bounds__(512) k_axis_reg(const AxisArgs<R> a0) {
 #pragma unroll
       for (int r = 0; r < F::R2; ++r) w[r] = buf[(j + F::R1 * r) * Tt + t];
 #pragma unroll
-      for (int r = 1; r < F::R2; ++r) w[r] = cmul(w[r], reg_tw<false>(a.ap.tw, j * r));
+      for (int r = 1; r < F::R2; ++r) w[r] = cmul(w[r], reg_tw<false>(tws, j * r));
       Dft<F::R2, false, T>::run(w);
       if (ok) {
 #pragma unroll
@@ -94,6 +108,7 @@ __global__ void __launch_bounds__(512) k_axis_reg(const AxisArgs<R> a0) {
       }
     }
   } else {
+    __syncthreads();  // the twiddle copy
 #pragma unroll
     for (int b = 0; b < F::NB; ++b) {
       const int j = y + F::Y * b;
@@ -102,7 +117,7 @@ __global__ void __launch_bounds__(512) k_axis_reg(const AxisArgs<R> a0) {
       for (int r = 0; r < F::R2; ++r) w[r] = ok ? base[(j + F::R1 * r) * se] : T{R(0), R(0)};
       Dft<F::R2, true, T>::run(w);
 #pragma unroll
-      for (int r = 1; r < F::R2; ++r) w[r] = cmul(w[r], reg_tw<true>(a.ap.tw, j * r));
+      for (int r = 1; r < F::R2; ++r) w[r] = cmul(w[r], reg_tw<true>(tws, j * r));
 #pragma unroll
       for (int r = 0; r < F::R2; ++r) buf[(j + F::R1 * r) * Tt + t] = w[r];
     }
@@ -148,6 +163,8 @@ __global__ void __launch_bounds__(384, 2) k_green_reg(const GreenArgs<R> a0) {
   T *base = a.spec + (long long)comp * a.nk + rho;
   const long long se = a.Rr;
   T *col = buf + z * Tt + t;  // this thread's pencil: slot s at col[s * P]
+  T *tws = buf + (size_t)P * M;  // after the tile
+  stage_twiddles<M>(tws, a.ap.tw);
   {
     T v[F::R1];
 #pragma unroll
@@ -164,7 +181,7 @@ __global__ void __launch_bounds__(384, 2) k_green_reg(const GreenArgs<R> a0) {
 #pragma unroll
     for (int r = 0; r < F::R2; ++r) w[r] = col[(j + F::R1 * r) * P];
 #pragma unroll
-    for (int r = 1; r < F::R2; ++r) w[r] = cmul(w[r], reg_tw<false>(a.ap.tw, j * r));
+    for (int r = 1; r < F::R2; ++r) w[r] = cmul(w[r], reg_tw<false>(tws, j * r));
     Dft<F::R2, false, T>::run(w);
 #pragma unroll
     for (int r = 0; r < F::R2; ++r) col[(j + F::R1 * r) * P] = w[r];  // X[j + R1 r], own slots
@@ -214,7 +231,7 @@ __global__ void __launch_bounds__(384, 2) k_green_reg(const GreenArgs<R> a0) {
     for (int r = 0; r < F::R2; ++r) w[r] = col[(j + F::R1 * r) * P];
     Dft<F::R2, true, T>::run(w);
 #pragma unroll
-    for (int r = 1; r < F::R2; ++r) w[r] = cmul(w[r], reg_tw<true>(a.ap.tw, j * r));
+    for (int r = 1; r < F::R2; ++r) w[r] = cmul(w[r], reg_tw<true>(tws, j * r));
 #pragma unroll
     for (int r = 0; r < F::R2; ++r) col[(j + F::R1 * r) * P] = w[r];
   }
@@ -263,6 +280,8 @@ __global__ void __launch_bounds__(512) k_last_fwd_reg(const LastArgs<float> a0) 
   if (!a.st->active) return;
   const int G = a.G, G2 = G >> 1, H = a.H;
   const int tid = threadIdx.x + blockDim.x * threadIdx.y, nth = blockDim.x * blockDim.y;
+  T *tws = buf + (size_t)a.ncomp * G2 * Lay::PS;  // after the pencils
+  stage_twiddles<M>(tws, a.ap.tw);
   const long long row0 = (long long)blockIdx.x * G;
   const bool first = a.st->iter == 0;
   const R beta = R(a.st->beta);
@@ -312,7 +331,7 @@ __global__ void __launch_bounds__(512) k_last_fwd_reg(const LastArgs<float> a0) 
 #pragma unroll
     for (int r = 0; r < F::R2; ++r) w[r] = col[Lay::pos(j + F::R1 * r)];
 #pragma unroll
-    for (int r = 1; r < F::R2; ++r) w[r] = cmul(w[r], reg_tw<false>(a.ap.tw, j * r));
+    for (int r = 1; r < F::R2; ++r) w[r] = cmul(w[r], reg_tw<false>(tws, j * r));
     Dft<F::R2, false, T>::run(w);
 #pragma unroll
     for (int r = 0; r < F::R2; ++r) col[Lay::pos(j + F::R1 * r)] = w[r];
@@ -356,6 +375,8 @@ __global__ void __launch_bounds__(384, 2) k_last_inv_reg(const LastArgs<float> a
   const long long ox = (long long)c * a.npx + rx * L, oy = ox + L;
   const T *sx = a.spec + (long long)c * a.nk + rx * H;
   T *col = buf + q * Lay::PS;
+  T *tws = buf + (size_t)a.ncomp * G2 * Lay::PS;  // after the pencils
+  stage_twiddles<M>(tws, a.ap.tw);
   // every spectrum entry of the lane first (the transform needs them), then p (the
   // epilogue needs it), so the spectrum loads are not queued behind the p loads
   T w[F::NB][F::R2];
@@ -386,12 +407,13 @@ __global__ void __launch_bounds__(384, 2) k_last_inv_reg(const LastArgs<float> a
     px[r] = okx ? a.p[ox + y + F::Y * r] : R(0);
     py[r] = oky ? a.p[oy + y + F::Y * r] : R(0);
   }
+  __syncthreads();  // the twiddle copy
 #pragma unroll
   for (int b = 0; b < F::NB; ++b) {
     const int j = y + F::Y * b;
     Dft<F::R2, true, T>::run(w[b]);
 #pragma unroll
-    for (int r = 1; r < F::R2; ++r) w[b][r] = cmul(w[b][r], reg_tw<true>(a.ap.tw, j * r));
+    for (int r = 1; r < F::R2; ++r) w[b][r] = cmul(w[b][r], reg_tw<true>(tws, j * r));
 #pragma unroll
     for (int r = 0; r < F::R2; ++r) col[Lay::pos(j + F::R1 * r)] = w[b][r];
   }

@@ -1,6 +1,8 @@
 // TMA-fed Green pass (FP32): the kernels of spectral_tma.cuh, their tensor-map
 // descriptors and launcher, and the device fault word of their bounded waits.
 #include <cstring>
+#include <map>
+#include <tuple>
 
 #include "spectral_launch.cuh"
 #include "spectral_tma.cuh"
@@ -56,7 +58,58 @@ template <int TT> GreenTmaKernel green_tma_kernel(int mode, int dim, int m) {
   return dim == 2 ? green_tma_kernel<GM_SMALL, 2, TT>(m) : green_tma_kernel<GM_SMALL, 3, TT>(m);
 }
 
+// resident blocks per SM x SMs for a kernel launch shape (cached; thread-safe)
+int persistent_grid(const void *k, int threads, size_t smem) {
+  static std::mutex mu;
+  static std::map<std::tuple<const void *, int, size_t>, int> cache;
+  std::lock_guard<std::mutex> lock(mu);
+  const auto key = std::make_tuple(k, threads, smem);
+  auto it = cache.find(key);
+  if (it != cache.end()) return it->second;
+  int per_sm = 0, dev = 0, nsm = 0;
+  MUSG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, threads, smem));
+  MUSG_CUDA(cudaGetDevice(&dev));
+  MUSG_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  const int g = per_sm * nsm;
+  cache[key] = g;
+  return g;
+}
+
+using LastInvTmaKernel = void (*)(const LastArgs<float>, unsigned);
+
+template <int D> LastInvTmaKernel last_inv_tma_kernel(int m) {
+  switch (m) {
+    case 16: return k_last_inv_tma<16, D>;
+    case 32: return k_last_inv_tma<32, D>;
+    case 64: return k_last_inv_tma<64, D>;
+    case 128: return k_last_inv_tma<128, D>;
+    case 256: return k_last_inv_tma<256, D>;
+    default: return nullptr;
+  }
+}
+
 }  // namespace
+
+// The staged rows need 16-byte aligned copies: an even row count (every tile, the
+// last one included, holds an even number of rows of H complex values), an even
+// number of k-points per plane and a 16-byte aligned spectrum.
+int launch_last_inv_tma(Spectral &sp, const LastArgs<float> &a, int G, cudaStream_t s) {
+  const int dim = sp.g.dim, m = sp.ax[dim - 1].m, Y = reg_lanes(m), nc = sp.ncomp;
+  if (nc != dim * dim || G % 2 || sp.g.nrows % 2 || sp.g.nk % 2 || (reinterpret_cast<uintptr_t>(sp.spec32) & 15))
+    return 0;
+  const LastInvTmaKernel k = dim == 2 ? last_inv_tma_kernel<2>(m) : last_inv_tma_kernel<3>(m);
+  const int threads = Y * nc * (G / 2);
+  const size_t smem = k_last_inv_tma_smem(m, nc, G);
+  if (!k || threads > 224 || smem > (size_t)optin_smem()) return 0;  // launch bounds of the kernel
+  allow_smem(k);
+  const int per_grid = persistent_grid((const void *)k, threads, smem);
+  if (per_grid < 1) return 0;
+  const long long ntiles = (sp.g.nrows + G - 1) / G;
+  const int grid = (int)std::min<long long>(ntiles, per_grid);
+  launch_pdl(k, dim3(grid), dim3(Y, nc * (G / 2)), smem, s, a, (unsigned)last_inv_tma_stage(m, nc, G));
+  MUSG_CHECK_LAUNCH();
+  return grid;
+}
 
 // The descriptor is 5-D over the FP32 spectrum [comp][e][rho]: (rho, row group,
 // component in the group, e div Y, e mod Y), box (Tt, 1, NC, R1, Y).  It needs a

@@ -32,6 +32,7 @@
 #pragma once
 
 #include <cuda.h>
+#include <algorithm>
 #include <cstdint>
 
 #include "spectral_reg.cuh"
@@ -271,6 +272,180 @@ __global__ void __launch_bounds__(384, 2) k_green_tma(const GreenArgs<float> a, 
       for (int r = 0; r < F::R1; ++r) base[(long long)(y + F::Y * r) * a.Rr] = v[r];
     }
   }
+}
+
+__device__ __forceinline__ void bulk_load(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(src)), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+
+// Last-axis inverse with the CG epilogue (the pass k_last_inv_reg computes), fed by
+// bulk copies: a persistent block walks tiles of G rows; one thread stages the next
+// tile's half spectra (per component the G rows are G*H contiguous complex values: one
+// cp.async.bulk of G*H*8 bytes each) while the block transforms the current tile.  A
+// lane reads all its spectrum entries of the tile into registers first, so after one
+// barrier the tile's stage doubles as the transform's exchange buffer and a block
+// needs two stages only.  The p entries are loaded from global memory at the start of
+// each tile (they are needed in the epilogue).  Each block sums p.Ap over its tiles
+// into one partial sum; the last block to finish computes alpha.
+// Dynamic shared memory: k_last_inv_tma_smem bytes.
+inline size_t last_inv_tma_stage(int m, int nc, int G) {
+  const size_t spec = (size_t)nc * G * (m / 2 + 1) * sizeof(float2);
+  const size_t xchg = (size_t)nc * (G / 2) * (m + m / (m == 16 ? 4 : (m == 32 || m == 64) ? 8 : 16)) * sizeof(float2);
+  return (std::max(spec, xchg) + 15) / 16 * 16;
+}
+inline size_t k_last_inv_tma_smem(int m, int nc, int G) {
+  return 2 * last_inv_tma_stage(m, nc, G) + 32 + (size_t)m * sizeof(float2);
+}
+
+template <int M, int D>
+__global__ void __maxnreg__(96) k_last_inv_tma(const LastArgs<float> a, unsigned stage_bytes) {
+  dep_wait();
+  using R = float;
+  using T = float2;
+  using F = RegFft<M>;
+  using Lay = LastLayout<M>;
+  constexpr int L = M;
+  constexpr int NC = D * D;
+  extern __shared__ __align__(128) unsigned char tma_smem[];
+  if (!a.st->active) return;
+  const int G = a.G, G2 = G >> 1, H = a.H;
+  const int y = threadIdx.x, q = threadIdx.y;
+  const int c = q / G2, g2 = q - c * G2;
+  const int tid = lin_tid();
+  uint64_t *bars = reinterpret_cast<uint64_t *>(tma_smem + 2 * (size_t)stage_bytes);
+  int &s_fault = *reinterpret_cast<int *>(bars + 2);
+  T *tw = reinterpret_cast<T *>(bars + 4);  // W_M^k, k < M
+  const long long ntiles = (a.nrows + G - 1) / G;
+  auto issue = [&](long long tile, int s) {
+    const long long row0 = tile * G;
+    const long long rows = a.nrows - row0 < G ? a.nrows - row0 : G;
+    const uint32_t bytes = (uint32_t)(rows * H * (long long)sizeof(T));
+    unsigned char *dst = tma_smem + (size_t)s * stage_bytes;
+    mbar_expect_tx(&bars[s], bytes * NC);
+    for (int cc = 0; cc < NC; ++cc)
+      bulk_load(dst + (size_t)cc * G * H * sizeof(T), a.spec + (long long)cc * a.nk + row0 * H, bytes, &bars[s]);
+  };
+  bool pending[2] = {false, false};
+  if (tid == 0) {
+    s_fault = 0;
+    mbar_init(&bars[0], 1);
+    mbar_init(&bars[1], 1);
+    mbar_init_fence();
+  }
+  for (int k = tid; k < M; k += lin_nth()) tw[k] = a.ap.tw[k];
+  __syncthreads();
+  long long tile = blockIdx.x;
+  if (tid == 0) {
+    if (tile < ntiles) {
+      issue(tile, 0);
+      pending[0] = true;
+    }
+    if (tile + gridDim.x < ntiles) {
+      issue(tile + gridDim.x, 1);
+      pending[1] = true;
+    }
+  }
+  Acc<R> acc;
+  for (int it = 0; tile < ntiles; ++it, tile += gridDim.x) {
+    const int s = it & 1;
+    const uint32_t parity = (uint32_t)((it >> 1) & 1);
+    const long long row0 = tile * G;
+    const long long rx = row0 + 2 * g2, ry = rx + 1;
+    const bool okx = rx < a.nrows, oky = ry < a.nrows;
+    const long long ox = (long long)c * a.npx + rx * L, oy = ox + L;
+    R px[F::R1], py[F::R1];
+#pragma unroll
+    for (int r = 0; r < F::R1; ++r) {
+      px[r] = okx ? a.p[ox + y + F::Y * r] : R(0);
+      py[r] = oky ? a.p[oy + y + F::Y * r] : R(0);
+    }
+    if (tid == 0) {
+      if (mbar_wait_bounded(&bars[s], parity)) {
+        pending[s] = false;
+      } else {
+        s_fault = 1;
+      }
+    }
+    __syncthreads();
+    if (s_fault) {
+      if (tid == 0) {
+        atomicOr(&g_wait_fault, 1u);
+        const_cast<CGState *>(a.st)->active = 0;
+        const uint32_t par1 = (uint32_t)(((it + 1) >> 1) & 1);
+        if (pending[s ^ 1]) (void)mbar_wait_bounded(&bars[s ^ 1], par1);
+      }
+      return;
+    }
+    (void)mbar_try_wait(&bars[s], parity);
+    T *stage = reinterpret_cast<T *>(tma_smem + (size_t)s * stage_bytes);
+    const T *sx = stage + ((size_t)c * G + 2 * g2) * H;
+    T w[F::NB][F::R2];
+#pragma unroll
+    for (int b = 0; b < F::NB; ++b) {
+      const int j = y + F::Y * b;
+#pragma unroll
+      for (int r = 0; r < F::R2; ++r) {
+        const int k = j + F::R1 * r;
+        const bool hi = k >= H;
+        const int kk = hi ? L - k : k;
+        T x = okx ? sx[kk] : T{R(0), R(0)};
+        T z = oky ? sx[H + kk] : T{R(0), R(0)};
+        if (hi) {
+          x.y = -x.y;
+          z.y = -z.y;
+        }
+        if (k == 0 || 2 * k == L) {  // c2r uses the real part of self-conjugate bins only
+          x.y = R(0);
+          z.y = R(0);
+        }
+        w[b][r] = T{x.x - z.y, x.y + z.x};
+      }
+    }
+    __syncthreads();  // the stage now serves as the exchange buffer
+    T *col = stage + q * Lay::PS;
+#pragma unroll
+    for (int b = 0; b < F::NB; ++b) {
+      const int j = y + F::Y * b;
+      Dft<F::R2, true, T>::run(w[b]);
+#pragma unroll
+      for (int r = 1; r < F::R2; ++r) {
+        const T u = tw[j * r];
+        w[b][r] = cmul(w[b][r], T{u.x, -u.y});
+      }
+#pragma unroll
+      for (int r = 0; r < F::R2; ++r) col[Lay::pos(j + F::R1 * r)] = w[b][r];
+    }
+    __syncthreads();
+    T v[F::R1];
+#pragma unroll
+    for (int r = 0; r < F::R1; ++r) v[r] = col[Lay::pos(y * F::R1 + r)];
+    __syncthreads();  // every thread is done with this stage
+    if (tid == 0 && tile + 2 * (long long)gridDim.x < ntiles) {
+      fence_proxy_async_smem();
+      issue(tile + 2 * (long long)gridDim.x, s);
+      pending[s] = true;
+    }
+    Dft<F::R1, true, T>::run(v);
+#pragma unroll
+    for (int r = 0; r < F::R1; ++r) {
+      const int e = y + F::Y * r;
+      if (okx) {
+        a.Ap[ox + e] = v[r].x;
+        acc.add(px[r] * v[r].x);
+      }
+      if (oky) {
+        a.Ap[oy + e] = v[r].y;
+        acc.add(py[r] * v[r].y);
+      }
+    }
+  }
+  const double bs = block_sum(acc.value());
+  if (tid == 0) a.partial[blockIdx.x] = bs;
+  CGState *st = const_cast<CGState *>(a.st);
+  if (cg_last_block(st)) cg_alpha_step(st, a.partial, gridDim.x);
 }
 
 }  // namespace musg

@@ -280,6 +280,13 @@ def run_stream(requests, rate_hz, server):
     wall = time.perf_counter() - t0
     lat = np.array([r.latency for r in server.results.values()])
     ok = sum(r.success for r in server.results.values())
+    laws = {req.rid: '+'.join(sorted({m[0] for m in req.materials})) for req in requests}
+    failed = {}
+    for rid, r in server.results.items():
+        if not r.success:
+            key = '%s: %s' % (laws.get(rid, '?'), r.message.split(' After ')[0][:60])
+            failed[key] = failed.get(key, 0) + 1
     return {'requests': len(requests), 'succeeded': int(ok), 'wall_s': wall, 'solves_per_s': len(requests) / wall,
+            'succeeded_per_s': int(ok) / wall, 'failed': failed,
             'p50_ms': float(np.percentile(lat, 50) * 1e3), 'p99_ms': float(np.percentile(lat, 99) * 1e3),
             'peak_hbm_bytes': server.peak_in_use, 'batches': server.admitted_batches}
