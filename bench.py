@@ -426,7 +426,7 @@ def main():
 
     # ---------------- end to end through the public API from host buffers
     e2e_t = []
-    h2d = npx * (1 + 2 * 8)  # material index byte + lambda, mu (FP64) per pixel
+    h2d = npx  # the material index byte per pixel (the Lame planes are filled on the device from it)
     d2h = d2 * 8             # the homogenised stress (the metric's result)
     for i in range(args.e2e_steps + 1):
         torch.cuda.synchronize()

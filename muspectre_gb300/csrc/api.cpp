@@ -40,6 +40,11 @@ template <typename F> int guard(F &&f) {
 void require(bool ok, int code, const std::string &msg) {
   if (!ok) throw Error(code, msg);
 }
+// literal messages: no std::string is built unless the check fails (some checks run
+// once per pixel)
+void require(bool ok, int code, const char *msg) {
+  if (!ok) throw Error(code, msg);
+}
 
 }  // namespace
 
@@ -263,7 +268,11 @@ struct musg_cell {
     require(materials.size() <= (size_t)kMaxMaterials, MUSG_ERR_ARGUMENT, "at most 256 materials per cell");
     check_material_coverage();
     std::vector<uint8_t> hmat(npx);
-    std::vector<double> hlam(npx), hmu(npx);
+    // per-pixel Lame constants on the host only for the laws that have them per pixel;
+    // the others are filled on the device from the material index
+    bool per_pixel_lame = false;
+    for (const Material &mt : materials) per_pixel_lame |= mt.law == MUSG_LAW_LE3 || mt.law == MUSG_LAW_LE4;
+    std::vector<double> hlam(per_pixel_lame ? npx : 0), hmu(per_pixel_lame ? npx : 0);
     std::vector<MatParams> hp(materials.size());
     std::vector<uint8_t> hkind(kMaxMaterials, TK_FINITE);
     bool any_le = false;
@@ -288,6 +297,7 @@ struct musg_cell {
       for (size_t k = 0; k < mt.pixels.size(); ++k) {
         const long long p = mt.pixels[k];
         hmat[p] = (uint8_t)m;
+        if (!per_pixel_lame) continue;
         if (mt.law == MUSG_LAW_LE3 || mt.law == MUSG_LAW_LE4) {
           const double E = mt.per_pixel[2 * k], nu = mt.per_pixel[2 * k + 1];
           hlam[p] = lame_lambda(E, nu);
@@ -333,8 +343,12 @@ struct musg_cell {
     MUSG_CUDA(cudaMemcpy(law_kind.p, hkind.data(), kMaxMaterials, cudaMemcpyHostToDevice));
     lam64.alloc(plane_bytes());
     mu64.alloc(plane_bytes());
-    MUSG_CUDA(cudaMemcpy(lam64.p, hlam.data(), plane_bytes(), cudaMemcpyHostToDevice));
-    MUSG_CUDA(cudaMemcpy(mu64.p, hmu.data(), plane_bytes(), cudaMemcpyHostToDevice));
+    if (per_pixel_lame) {
+      MUSG_CUDA(cudaMemcpy(lam64.p, hlam.data(), plane_bytes(), cudaMemcpyHostToDevice));
+      MUSG_CUDA(cudaMemcpy(mu64.p, hmu.data(), plane_bytes(), cudaMemcpyHostToDevice));
+    } else {
+      fill_lame(mat.as<uint8_t>(), params.as<MatParams>(), lam64.as<double>(), mu64.as<double>(), npx, stream);
+    }
     if (has_le2) {
       std::vector<double> h((size_t)npx * D2, 0.0);
       for (const Material &mt : materials)
@@ -1204,11 +1218,12 @@ int musg_material_add_pixels(musg_cell *cell, int material, const long long *pix
         require(per_pixel && stride == m.stride, MUSG_ERR_RUNTIME,
                 "this material needs pixels with Youngs modulus and Poisson ratio.");
     }
-    for (long long k = 0; k < count; ++k) {
-      require(pixels[k] >= 0 && pixels[k] < cell->npx, MUSG_ERR_ARGUMENT, "pixel index out of range");
-      m.pixels.push_back(pixels[k]);
-      for (int s = 0; s < m.stride; ++s) m.per_pixel.push_back(per_pixel[k * stride + s]);
-    }
+    require(count >= 0 && (count == 0 || pixels), MUSG_ERR_ARGUMENT, "null pixel list");
+    bool in_range = true;
+    for (long long k = 0; k < count; ++k) in_range &= pixels[k] >= 0 && pixels[k] < cell->npx;
+    require(in_range, MUSG_ERR_ARGUMENT, "pixel index out of range");
+    m.pixels.insert(m.pixels.end(), pixels, pixels + count);
+    if (m.stride > 0) m.per_pixel.insert(m.per_pixel.end(), per_pixel, per_pixel + count * (long long)m.stride);
   });
 }
 

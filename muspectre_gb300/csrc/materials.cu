@@ -502,7 +502,21 @@ int grid_for(long long n, int threads) {
   return (int)(b < 1 ? 1 : b);
 }
 
+__global__ void k_fill_lame(const uint8_t *__restrict__ mat, const MatParams *__restrict__ params, double *lam,
+                            double *mu, long long npx) {
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < npx; p += (long long)gridDim.x * blockDim.x) {
+    const MatParams &q = params[mat[p]];
+    lam[p] = q.lam;
+    mu[p] = q.mu;
+  }
+}
+
 }  // namespace
+
+void fill_lame(const uint8_t *mat, const MatParams *params, double *lam, double *mu, long long npx, cudaStream_t s) {
+  k_fill_lame<<<grid_for(npx, 256), 256, 0, s>>>(mat, params, lam, mu, npx);
+  MUSG_CHECK_LAUNCH();
+}
 
 void material_evaluate(const MaterialArgs &a, cudaStream_t s) {
   const int nb = (int)((a.npx + kMatThreads - 1) / kMatThreads);

@@ -294,6 +294,8 @@ struct MaterialArgs {
 void material_evaluate(const MaterialArgs &a, cudaStream_t s);
 void add_macro(double *F, const double *delta_dev, int ncomp, long long npx, cudaStream_t s);
 void fill_uniform(double *F, const double *value_dev, int ncomp, long long npx, cudaStream_t s);
+// per-pixel Lame planes from the material index and the per-material parameters
+void fill_lame(const uint8_t *mat, const MatParams *params, double *lam, double *mu, long long npx, cudaStream_t s);
 
 // AoS (host layout, pixel-major) <-> SoA (component planes) on the device
 void aos_to_soa(const double *aos, double *soa, int ncomp, long long npx, cudaStream_t s);

@@ -161,11 +161,16 @@ __device__ __forceinline__ void tangent_finite(const R *dF, const R *F, const R 
   R tr = R(0);
 #pragma unroll
   for (int i = 0; i < D; ++i) tr += A[i + D * i];
+  // B is symmetric: the (m, r) entry repeats the (r, m) one bit for bit
   R B[D * D];
 #pragma unroll
   for (int m = 0; m < D; ++m)
 #pragma unroll
-    for (int r = 0; r < D; ++r) B[r + D * m] = mu * (A[r + D * m] + A[m + D * r]) + (r == m ? lam * tr : R(0));
+    for (int r = 0; r <= m; ++r) {
+      const R b = mu * (A[r + D * m] + A[m + D * r]) + (r == m ? lam * tr : R(0));
+      B[r + D * m] = b;
+      B[m + D * r] = b;
+    }
 #pragma unroll
   for (int m = 0; m < D; ++m)
 #pragma unroll
@@ -287,23 +292,30 @@ template <int D, int TK, typename R> struct TangentLocal {
   __device__ __forceinline__ void finish() {
     if constexpr (kFinite && sizeof(R) == 4) {
       if constexpr (TK == TK_FISO) {
+        // E and S are symmetric: each (j, i) entry repeats the (i, j) one bit for bit
         R E[D2];
         R tr = R(0);
 #pragma unroll
         for (int j = 0; j < D; ++j)
 #pragma unroll
-          for (int i = 0; i < D; ++i) {
+          for (int i = 0; i <= j; ++i) {
             R hh = R(0);
 #pragma unroll
             for (int k = 0; k < D; ++k) hh += F[k + D * i] * F[k + D * j];
-            E[i + D * j] = R(0.5) * (F[i + D * j] + F[j + D * i] + hh);
+            const R e = R(0.5) * (F[i + D * j] + F[j + D * i] + hh);
+            E[i + D * j] = e;
+            E[j + D * i] = e;
           }
 #pragma unroll
         for (int i = 0; i < D; ++i) tr += E[i + D * i];
 #pragma unroll
         for (int j = 0; j < D; ++j)
 #pragma unroll
-          for (int i = 0; i < D; ++i) S[i + D * j] = R(2) * mu * E[i + D * j] + (i == j ? lam * tr : R(0));
+          for (int i = 0; i <= j; ++i) {
+            const R sv = R(2) * mu * E[i + D * j] + (i == j ? lam * tr : R(0));
+            S[i + D * j] = sv;
+            S[j + D * i] = sv;
+          }
       }
       if (TK != TK_MIXED || kind == TK_FINITE) {
 #pragma unroll

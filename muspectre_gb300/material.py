@@ -40,7 +40,8 @@ class _Material:
     def _flush(self):
         if not self._pending_idx:
             return
-        idx = np.ascontiguousarray(np.concatenate(self._pending_idx).astype(np.int64))
+        idx = self._pending_idx[0] if len(self._pending_idx) == 1 else np.concatenate(self._pending_idx)
+        idx = np.ascontiguousarray(idx, dtype=np.int64)
         vals = None
         if self._stride():
             vals = np.ascontiguousarray(np.concatenate(self._pending_val).astype(np.float64))
