@@ -451,6 +451,7 @@ struct musg_cell {
       a.Kfull = Kfull.as<double>();
     }
     a.nonfinite = nonfinite.as<int>();
+    a.has_hep = has_hep ? 1 : 0;
     material_evaluate(a, stream);
     tangent_valid = true;
   }

@@ -222,7 +222,10 @@ template <int D> __device__ __forceinline__ M<D> expm_sym(const M<D> &T) {
 
 template <typename R> __device__ __forceinline__ void store(R *p, long long o, double v) { p[o] = (R)v; }
 
-template <int D>
+// HEP: the cell has MaterialHyperElastoPlastic1 pixels.  Without them the elasto-plastic
+// branch (eigen-solves, logm/expm) is compiled out, which keeps the elastic laws at a
+// fraction of its registers (164 with it), so more blocks are resident.
+template <int D, bool HEP>
 __global__ void __launch_bounds__(kMatThreads) k_material(const MaterialArgs a, int cur) {
   constexpr int D2 = D * D;
   const long long px = blockIdx.x * (long long)blockDim.x + threadIdx.x;
@@ -234,7 +237,7 @@ __global__ void __launch_bounds__(kMatThreads) k_material(const MaterialArgs a, 
   const MatParams mp = a.params[a.mat[px]];
   M<D> P;
   const bool finite = (a.form == MUSG_FINITE_STRAIN);
-  if (mp.law != MUSG_LAW_HEP1) {
+  if (!HEP || mp.law != MUSG_LAW_HEP1) {
     const double lam = a.lam[px], mu = a.mu[px];
     // strain measure: infinitesimal (small) or Green-Lagrange (finite)
     M<D> E;
@@ -520,8 +523,13 @@ void fill_lame(const uint8_t *mat, const MatParams *params, double *lam, double 
 
 void material_evaluate(const MaterialArgs &a, cudaStream_t s) {
   const int nb = (int)((a.npx + kMatThreads - 1) / kMatThreads);
-  if (a.dim == 2) k_material<2><<<nb, kMatThreads, 0, s>>>(a, a.cur);
-  else k_material<3><<<nb, kMatThreads, 0, s>>>(a, a.cur);
+  if (a.dim == 2) {
+    if (a.has_hep) k_material<2, true><<<nb, kMatThreads, 0, s>>>(a, a.cur);
+    else k_material<2, false><<<nb, kMatThreads, 0, s>>>(a, a.cur);
+  } else {
+    if (a.has_hep) k_material<3, true><<<nb, kMatThreads, 0, s>>>(a, a.cur);
+    else k_material<3, false><<<nb, kMatThreads, 0, s>>>(a, a.cur);
+  }
   MUSG_CHECK_LAUNCH();
 }
 

@@ -290,6 +290,7 @@ struct MaterialArgs {
   float *S32, *Kp32, *Fc32;
   double *Kfull;            // optional full tangent, AoS [npx][D^4] (API)
   int *nonfinite;           // device flag set when a non-finite stress appears
+  int has_hep;              // any MaterialHyperElastoPlastic1 pixel in the cell
 };
 void material_evaluate(const MaterialArgs &a, cudaStream_t s);
 void add_macro(double *F, const double *delta_dev, int ncomp, long long npx, cudaStream_t s);
