@@ -19,7 +19,7 @@ bool launch_green_tma(Spectral &sp, int mode, const GreenArgs<float> &a, int Tt,
 // The FP32 last-axis inverse with the CG epilogue through the bulk-copy-fed
 // persistent kernel (spectral_tma.cu) for tiles of G rows; returns its number of
 // blocks (= partial sums), or 0 (nothing launched) when the shape does not qualify.
-int launch_last_inv_tma(Spectral &sp, const LastArgs<float> &a, int G, cudaStream_t s);
+int launch_last_inv_tma(Spectral &sp, const LastArgs<float> &a, int G, cudaStream_t s, int B = 1);
 
 namespace {
 
@@ -300,8 +300,8 @@ int last_cg_reg(Spectral &sp, int tkind, LastArgs<R> a, int G, bool inv, cudaStr
 #undef MUSG_FR
       throw Error(MUSG_ERR_ARGUMENT, "unsupported tangent kind");
     }
-    if (B == 1 && !a.batch) {
-      const int nb = launch_last_inv_tma(sp, a, G, s);
+    {
+      const int nb = launch_last_inv_tma(sp, a, G, s, B);
       if (nb) return nb;
     }
     if (sp.g.dim == 2) launch_inv_reg<2>(m, a, grid, block, smem, s);

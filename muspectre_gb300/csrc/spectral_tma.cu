@@ -92,8 +92,9 @@ template <int D> LastInvTmaKernel last_inv_tma_kernel(int m) {
 
 // The staged rows need 16-byte aligned copies: an even row count (every tile, the
 // last one included, holds an even number of rows of H complex values), an even
-// number of k-points per plane and a 16-byte aligned spectrum.
-int launch_last_inv_tma(Spectral &sp, const LastArgs<float> &a, int G, cudaStream_t s) {
+// number of k-points per plane and 16-byte aligned spectra (cudaMalloc'd; a batch's
+// problems share the grid, so the host checks the first one).
+int launch_last_inv_tma(Spectral &sp, const LastArgs<float> &a, int G, cudaStream_t s, int B) {
   const int dim = sp.g.dim, m = sp.ax[dim - 1].m, Y = reg_lanes(m), nc = sp.ncomp;
   if (nc != dim * dim || G % 2 || sp.g.nrows % 2 || sp.g.nk % 2 || (reinterpret_cast<uintptr_t>(sp.spec32) & 15))
     return 0;
@@ -106,7 +107,7 @@ int launch_last_inv_tma(Spectral &sp, const LastArgs<float> &a, int G, cudaStrea
   if (per_grid < 1) return 0;
   const long long ntiles = (sp.g.nrows + G - 1) / G;
   const int grid = (int)std::min<long long>(ntiles, per_grid);
-  launch_pdl(k, dim3(grid), dim3(Y, nc * (G / 2)), smem, s, a, (unsigned)last_inv_tma_stage(m, nc, G));
+  launch_pdl(k, dim3(grid, B), dim3(Y, nc * (G / 2)), smem, s, a, (unsigned)last_inv_tma_stage(m, nc, G));
   MUSG_CHECK_LAUNCH();
   return grid;
 }

@@ -289,8 +289,10 @@ __device__ __forceinline__ void bulk_load(void *dst, const void *src, uint32_t b
 // barrier the tile's stage doubles as the transform's exchange buffer and a block
 // needs two stages only.  The p entries are loaded from global memory at the start of
 // each tile (they are needed in the epilogue).  Each block sums p.Ap over its tiles
-// into one partial sum; the last block to finish computes alpha.
-// Dynamic shared memory: k_last_inv_tma_smem bytes.
+// into one partial sum; the last block to finish computes alpha.  A batched launch
+// (a.batch) runs problem blockIdx.y with its own pointers, state and partial sums, in
+// the same order as a single-problem launch, so batched and solo results agree bit for
+// bit.  Dynamic shared memory: k_last_inv_tma_smem bytes.
 inline size_t last_inv_tma_stage(int m, int nc, int G) {
   const size_t spec = (size_t)nc * G * (m / 2 + 1) * sizeof(float2);
   const size_t xchg = (size_t)nc * (G / 2) * (m + m / (m == 16 ? 4 : (m == 32 || m == 64) ? 8 : 16)) * sizeof(float2);
@@ -301,8 +303,10 @@ inline size_t k_last_inv_tma_smem(int m, int nc, int G) {
 }
 
 template <int M, int D>
-__global__ void __maxnreg__(96) k_last_inv_tma(const LastArgs<float> a, unsigned stage_bytes) {
+__global__ void __maxnreg__(96) k_last_inv_tma(const LastArgs<float> a0, unsigned stage_bytes) {
   dep_wait();
+  LastArgs<float> a = a0;
+  a.bind();  // problem blockIdx.y of a batched launch
   using R = float;
   using T = float2;
   using F = RegFft<M>;

@@ -25,14 +25,18 @@ def _cells(mu, n, seeds, form='finite'):
     return out
 
 
+# 24^3: generic passes; 32^3: register passes, where a solo mixed solve runs the
+# TMA-fed Green and last-axis inverse kernels and a batched one the register Green
+# kernel and the batched TMA inverse (same arithmetic, same reduction order)
+@pytest.mark.parametrize('n', [24, 32])
 @pytest.mark.parametrize('precision', ['fp64', 'mixed'])
-def test_batch_equals_solo(mu, precision):
-    cells = _cells(mu, 24, [1, 2, 3])
+def test_batch_equals_solo(mu, precision, n):
+    cells = _cells(mu, n, [1, 2, 3])
     load = cells[0][1]['load']
     batch = mu.batch.BatchSolver([c for c, _ in cells], 1e-8, 2000, precision=precision)
     rb = batch.newton_cg(load, 1e-6, 0.0)
     for (c, w), res in zip(cells, rb):
-        solo_cell = _cells(mu, 24, [w['seed']])[0][0]
+        solo_cell = _cells(mu, n, [w['seed']])[0][0]
         rs = mu.solvers.newton_cg(solo_cell, load, mu.solvers.SolverCG(solo_cell, 1e-8, 2000, precision=precision),
                                   1e-6, 0.0)
         r = res[0]

@@ -130,6 +130,11 @@ OPERATOR_CASES = {
     'finite_le1_generic': dict(res=[15, 9, 10], form=0, law='le1'),         # generic (non power-of-two) passes
     'small_le1_generic': dict(res=[24, 20, 18], form=1, law='le1'),
     'finite_hep1_le1_generic': dict(res=[9, 7, 12], form=0, law='hep1+le1'),
+    # qualification rules of the TMA-fed kernels: an odd row count keeps the register
+    # last-axis inverse; an odd k-plane count keeps the register Green kernel
+    'finite_le1_odd_rows': dict(res=[9, 7, 16], form=0, law='le1'),
+    'finite_le1_odd_planes': dict(res=[16, 7, 32], form=0, law='le1'),
+    'small_le1_tma_both': dict(res=[32, 16, 32], form=1, law='le1'),
 }
 
 
