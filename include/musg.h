@@ -88,6 +88,11 @@ int musg_device_count(int *count);
 /* device used by the objects the calling thread creates afterwards (one process per
  * GPU; no counterpart in the reference, whose ranks are MPI processes) */
 int musg_set_device(int device);
+/* self-test of the bounded waits of the TMA-fed passes (no counterpart in the
+ * reference): one block waits on an mbarrier that nothing completes, gives up after
+ * limit_ms, and sets the device fault word; the host reads it the way it does after
+ * every FP32 CG solve, clears it, and reports *timed_out = 1.  The device stays usable. */
+int musg_selftest_wait_timeout(double limit_ms, int *timed_out);
 
 /* -------------------------------------------------------------- cell
  * make_cell<D,D>(res, lengths, form) (src/cell/cell_factory.hh:93-105) and

@@ -71,6 +71,7 @@ _LL = C.POINTER(C.c_longlong)
 _SIGNATURES = {
     'musg_last_error': (C.c_char_p, []),
     'musg_version': (C.c_int, []),
+    'musg_selftest_wait_timeout': (C.c_int, [C.c_double, C.POINTER(C.c_int)]),
     'musg_device_count': (C.c_int, [_I]),
     'musg_set_device': (C.c_int, [C.c_int]),
     'musg_cell_create': (C.c_int, [C.c_int, _I, _D, C.c_int, C.c_int, C.POINTER(_P)]),
@@ -191,6 +192,15 @@ def launch_count():
     n = C.c_ulonglong(0)
     check(lib().musg_launch_count(C.byref(n)))
     return n.value
+
+
+def selftest_wait_timeout(limit_ms=5.0):
+    """Self-test of the bounded mbarrier waits of the TMA-fed passes: True when a wait
+    that nothing completes gave up after ``limit_ms`` and the host saw the fault word
+    (musg_selftest_wait_timeout)."""
+    out = C.c_int(0)
+    check(lib().musg_selftest_wait_timeout(float(limit_ms), C.byref(out)))
+    return bool(out.value)
 
 
 def device_count():

@@ -1112,6 +1112,27 @@ const char *musg_last_error(void) { return g_last_error.c_str(); }
 
 int musg_version(void) { return 100; }
 
+int musg_selftest_wait_timeout(double limit_ms, int *timed_out) {
+  return guard([&] {
+    require(timed_out && limit_ms > 0 && limit_ms < 10000, MUSG_ERR_ARGUMENT, "limit_ms in (0, 10000) and an output");
+    cudaStream_t s = nullptr;
+    MUSG_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    unsigned fault = 0;
+    try {
+      MUSG_CUDA(cudaMemsetAsync(wait_fault_word(), 0, sizeof fault, s));
+      wait_probe((unsigned long long)(limit_ms * 1e6), s);
+      MUSG_CUDA(cudaMemcpyAsync(&fault, wait_fault_word(), sizeof fault, cudaMemcpyDeviceToHost, s));
+      MUSG_CUDA(cudaMemsetAsync(wait_fault_word(), 0, sizeof fault, s));
+      MUSG_CUDA(cudaStreamSynchronize(s));
+    } catch (...) {
+      cudaStreamDestroy(s);
+      throw;
+    }
+    cudaStreamDestroy(s);
+    *timed_out = fault ? 1 : 0;
+  });
+}
+
 int musg_set_device(int device) {
   return guard([&] { MUSG_CUDA(cudaSetDevice(device)); });
 }

@@ -183,6 +183,9 @@ struct Spectral {
 // Device word set by a kernel whose bounded wait on an asynchronous copy ran out
 // (spectral_tma.cuh); its device address, for a stream-ordered read by the host
 unsigned *wait_fault_word();
+// one block that waits on an mbarrier nothing arrives at, bounded by limit_ns
+// (self-test of the bounded waits: it sets the fault word and exits)
+void wait_probe(unsigned long long limit_ns, cudaStream_t s);
 
 // Launch configuration limits of the pass kernels
 constexpr int kPassThreads = 512;

@@ -9,6 +9,11 @@
 
 namespace musg {
 
+void wait_probe(unsigned long long limit_ns, cudaStream_t s) {
+  k_wait_probe<<<1, 32, 0, s>>>(limit_ns);
+  MUSG_CHECK_LAUNCH();
+}
+
 unsigned *wait_fault_word() {
   static unsigned *p = [] {
     void *q = nullptr;

@@ -79,12 +79,26 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
   return done != 0;
 }
 // poll until the phase of the given parity completed or the wall-clock limit ran out
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity) {
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity,
+                                                  unsigned long long limit_ns = kWaitLimitNs) {
   const unsigned long long t0 = global_ns();
   for (unsigned i = 0;; ++i) {
     if (mbar_try_wait(bar, parity)) return true;
-    if ((i & 255u) == 255u && global_ns() - t0 > kWaitLimitNs) return false;
+    if ((i & 255u) == 255u && global_ns() - t0 > limit_ns) return false;
   }
+}
+
+// Self-test of the bounded wait: one thread waits on an mbarrier that nothing arrives
+// at, gives up after limit_ns, records the fault word like the pass kernels do, and
+// the kernel exits (no copy is in flight).
+__global__ void k_wait_probe(unsigned long long limit_ns) {
+  __shared__ uint64_t bar;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    mbar_init_fence();
+  }
+  __syncthreads();
+  if (threadIdx.x == 0 && !mbar_wait_bounded(&bar, 0, limit_ns)) atomicOr(&g_wait_fault, 1u);
 }
 // generic-proxy accesses of shared memory before this point are ordered before the
 // async-proxy (TMA) accesses issued after it
