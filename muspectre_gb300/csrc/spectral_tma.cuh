@@ -4,10 +4,10 @@
 // thread while the block transforms the previous tile (two buffers, one mbarrier each).
 //
 // The register Green kernel (k_green_reg) loads a tile into registers, transforms it
-// and stores it; with two blocks per SM (80 registers per thread) the blocks' load,
-// transform and store phases line up and the SM alternates between waiting on HBM and
-// computing.  Here the next tile is in flight during the whole transform of the current
-// one, so HBM and the FFT arithmetic overlap inside each block.
+// and stores it.  Here the next tile is in flight during the whole transform of the
+// current one, so no thread holds load registers or waits on HBM latency; what bounds
+// the pass is then instruction issue (two FFTs per element), which the shared twiddle
+// table, the shared xi_0 and the compile-time tile width below reduce.
 //
 // Tile layout.  The tensor map splits the pencil index e = e_lo + Y e_hi (Y = M / R1
 // lanes) into two dimensions ordered (rho, row group, component, e_hi, e_lo), so the
