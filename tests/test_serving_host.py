@@ -85,3 +85,41 @@ def test_c5_generator_ranges():
             assert 1 <= len(r.steps) <= 10
         for s in r.steps:
             assert np.allclose(s, s.T) and np.all(np.abs(s) <= 0.02 + 1e-12)
+
+
+def test_stream_report_groups_failures_by_law():
+    """run_stream's report: throughput over all requests and over the solved ones, and the
+    failures grouped by the request's laws and the message's first sentence (a stand-in
+    server; no GPU)."""
+    reqs = [serving.c5_request(i, 2000 + i, small=True) for i in range(6)]
+
+    class FakeServer:
+        peak_in_use = 123
+        admitted_batches = 1
+
+        def __init__(self):
+            self.results = {}
+
+        def start(self):
+            pass
+
+        def submit(self, req):
+            ok = req.rid % 3 != 0
+            msg = '' if ok else 'Conjugate gradient has not converged. After 12 steps, the solver  FAILED'
+            self.results[req.rid] = serving.Result(req.rid, ok, msg, 1, 10, np.zeros((2, 2)), 0.01)
+
+        def close(self):
+            pass
+
+        def join(self):
+            pass
+
+    st = serving.run_stream(reqs, rate_hz=0.0, server=FakeServer())
+    assert st['requests'] == 6 and st['succeeded'] == 4
+    assert st['succeeded_per_s'] <= st['solves_per_s']
+    assert sum(st['failed'].values()) == 2
+    for key in st['failed']:
+        law, msg = key.split(': ', 1)
+        assert msg == 'Conjugate gradient has not converged.'
+        assert set(law.split('+')) <= {'le1', 'le4', 'hep1'}
+    assert st['peak_hbm_bytes'] == 123 and st['batches'] == 1
