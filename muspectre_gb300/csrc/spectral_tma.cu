@@ -82,13 +82,13 @@ int persistent_grid(const void *k, int threads, size_t smem) {
 
 using LastInvTmaKernel = void (*)(const LastArgs<float>, unsigned);
 
-template <int D> LastInvTmaKernel last_inv_tma_kernel(int m) {
+template <int D, bool BATCH> LastInvTmaKernel last_inv_tma_kernel(int m) {
   switch (m) {
-    case 16: return k_last_inv_tma<16, D>;
-    case 32: return k_last_inv_tma<32, D>;
-    case 64: return k_last_inv_tma<64, D>;
-    case 128: return k_last_inv_tma<128, D>;
-    case 256: return k_last_inv_tma<256, D>;
+    case 16: return k_last_inv_tma<16, D, BATCH>;
+    case 32: return k_last_inv_tma<32, D, BATCH>;
+    case 64: return k_last_inv_tma<64, D, BATCH>;
+    case 128: return k_last_inv_tma<128, D, BATCH>;
+    case 256: return k_last_inv_tma<256, D, BATCH>;
     default: return nullptr;
   }
 }
@@ -103,7 +103,9 @@ int launch_last_inv_tma(Spectral &sp, const LastArgs<float> &a, int G, cudaStrea
   const int dim = sp.g.dim, m = sp.ax[dim - 1].m, Y = reg_lanes(m), nc = sp.ncomp;
   if (nc != dim * dim || G % 2 || sp.g.nrows % 2 || sp.g.nk % 2 || (reinterpret_cast<uintptr_t>(sp.spec32) & 15))
     return 0;
-  const LastInvTmaKernel k = dim == 2 ? last_inv_tma_kernel<2>(m) : last_inv_tma_kernel<3>(m);
+  const bool batch = a.batch != nullptr;
+  const LastInvTmaKernel k = dim == 2 ? (batch ? last_inv_tma_kernel<2, true>(m) : last_inv_tma_kernel<2, false>(m))
+                                      : (batch ? last_inv_tma_kernel<3, true>(m) : last_inv_tma_kernel<3, false>(m));
   const int threads = Y * nc * (G / 2);
   const size_t smem = k_last_inv_tma_smem(m, nc, G);
   if (!k || threads > 224 || smem > (size_t)optin_smem()) return 0;  // launch bounds of the kernel

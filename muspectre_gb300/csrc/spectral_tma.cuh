@@ -316,11 +316,18 @@ inline size_t k_last_inv_tma_smem(int m, int nc, int G) {
   return 2 * last_inv_tma_stage(m, nc, G) + 32 + (size_t)m * sizeof(float2);
 }
 
-template <int M, int D>
+template <int M, int D, bool BATCH>
 __global__ void __maxnreg__(96) k_last_inv_tma(const LastArgs<float> a0, unsigned stage_bytes) {
   dep_wait();
-  LastArgs<float> a = a0;
-  a.bind();  // problem blockIdx.y of a batched launch
+  // a batched launch binds problem blockIdx.y's pointers; a single problem reads its
+  // arguments straight from the parameter space (no register copy, no spill at the
+  // 96-register cap)
+  LastArgs<float> ab;
+  if constexpr (BATCH) {
+    ab = a0;
+    ab.bind();
+  }
+  const LastArgs<float> &a = BATCH ? ab : a0;
   using R = float;
   using T = float2;
   using F = RegFft<M>;
