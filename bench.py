@@ -39,13 +39,21 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-# Newton and CG iteration counts of the FP64 method on the 128^3 seeded input
-# (identical between the oracle and the GPU FP64 path, as the parity tests check);
-# the CPU runs time a bounded sample and scale by them
+# Newton steps and CG iterations of a complete FP64 oracle solve of the 128^3 workload
+# (the reference's algorithm on the CPU), measured with
+#   python bench.py --impl reference --ref-full --steps 1 --warmup 0
+# The reference arm and the CPU baseline time a bounded sample (the Newton-level work
+# once, REF_SAMPLE_CG_ITERS CG iterations per step) and scale it by these counts.
 REF_NEWTON_STEPS = 4
 REF_CG_ITERS = 530
+REF_SAMPLE_CG_ITERS = 8
 # at or below this resolution the reference arm times complete oracle solves instead
 REF_FULL_SOLVE_MAX_N = 48
+
+
+def metric_name(n):
+    """The metric both arms report (the driver divides one arm's value by the other's)."""
+    return 'RVE solves/s (Newton-CG, %d^3 finite-strain LE1, 40 spheres)' % n
 
 
 def parse():
@@ -57,7 +65,9 @@ def parse():
     ap.add_argument('--n', type=int, default=128)
     ap.add_argument('--fp64-steps', type=int, default=2)
     ap.add_argument('--e2e-steps', type=int, default=2)
-    ap.add_argument('--cpu-cg-iters', type=int, default=4)
+    ap.add_argument('--cpu-cg-iters', type=int, default=REF_SAMPLE_CG_ITERS)
+    ap.add_argument('--ref-full', action='store_true',
+                    help='reference arm: complete oracle solves at any resolution (prints their counts)')
     ap.add_argument('--no-cpu', action='store_true')
     ap.add_argument('--no-extra', action='store_true', help='skip the other workloads (configs) of the metric')
     ap.add_argument('--only', default='all', choices=['all', 'mixed'],
@@ -157,7 +167,7 @@ def algorithmic_bytes(name, npx, nk, d2, s, tm):
 
 def measured_traffic(kernel, n):
     """DRAM bytes (read + write) per launch of a CG-iteration kernel from the committed
-    ncu capture of this workload (profiles/dram_spheres128_mixed.md), or None."""
+    ncu capture of this workload (profiles/traffic_spheres128_mixed.json), or None."""
     path = os.path.join(ROOT, 'profiles', 'traffic_spheres128_mixed.json')
     if n != 128 or not os.path.exists(path):
         return None
@@ -204,10 +214,11 @@ class CpuSample:
                           % (nit, self.res[0], newton_steps, cg_iters)}
 
 
-def cpu_baseline(w, newton_steps, cg_iters, nit):
-    """One bounded CPU sample of the workload (see CpuSample)."""
+def cpu_baseline(w, nit):
+    """One bounded CPU sample of the workload (see CpuSample), scaled by the oracle's
+    own Newton and CG counts of a complete solve."""
     smp = CpuSample(w)
-    return smp.describe(smp.cg_iteration_seconds(nit), newton_steps, cg_iters, nit)
+    return smp.describe(smp.cg_iteration_seconds(nit), REF_NEWTON_STEPS, REF_CG_ITERS, nit)
 
 
 def extra_configs(mu, workloads):
@@ -286,40 +297,53 @@ def extra_configs(mu, workloads):
 
 def run_reference(args, rank, world):
     """The reference's algorithm on the host CPU (the oracle; the C++ reference needs
-    Eigen and FFTW, absent here), same workload and metric."""
+    Eigen and FFTW, absent here), same workload and metric.  Up to 48^3 (or with
+    --ref-full) one step is one complete newton_cg solve; above, one step is a timed
+    sample of REF_SAMPLE_CG_ITERS CG iterations (after the Newton-level work, timed
+    once), and the value is the solve rate that sample gives at the oracle's counts."""
     if rank != 0:
         return
     from muspectre_gb300 import workloads
     w = workloads.spheres(args.n)
-    vals = []
+    vals, step_ms = [], []
     info = None
-    if args.n <= REF_FULL_SOLVE_MAX_N:
-        # small grids: one step = one complete oracle newton_cg solve
+    if args.n <= REF_FULL_SOLVE_MAX_N or args.ref_full:
         from oracle import muspectre_oracle as o
+        o.FFT_WORKERS = os.cpu_count() or 1
+        counts = None
         for step in range(args.warmup + args.steps):
             t0 = time.perf_counter()
             oc = workloads.build_spheres_oracle(o, w)
-            o.newton_cg(oc, w['load'], o.SolverCG(oc, w['cg_tol'], w['maxiter']), w['newton_tol'], w['equil_tol'], 0)
+            r = o.newton_cg(oc, w['load'], o.SolverCG(oc, w['cg_tol'], w['maxiter']), w['newton_tol'],
+                            w['equil_tol'], 0)
+            dt = time.perf_counter() - t0
+            counts = (r.nb_it, r.nb_fev)
             if step >= args.warmup:
-                vals.append(1.0 / (time.perf_counter() - t0))
-        info = {'cores': os.cpu_count() or 1, 'sample': 'complete solves at %d^3 (FP64)' % args.n}
+                vals.append(1.0 / dt)
+                step_ms.append(1e3 * dt)
+        info = {'cores': o.FFT_WORKERS, 'sample': 'complete solves at %d^3 (FP64): %d Newton steps, %d CG iterations'
+                % (args.n, counts[0], counts[1]), 'value_kind': 'timed complete solves'}
     else:
-        # the 128^3 FP64 counts; other large grids borrow them (the sample says so)
-        ns, nc = REF_NEWTON_STEPS, REF_CG_ITERS
         smp = CpuSample(w)  # the cell and one Newton-level evaluation, timed once
+        nit = args.cpu_cg_iters
         for step in range(args.warmup + args.steps):
-            info = smp.describe(smp.cg_iteration_seconds(1), ns, nc, 1)  # one step = one CG iteration sample
+            t0 = time.perf_counter()
+            info = smp.describe(smp.cg_iteration_seconds(nit), REF_NEWTON_STEPS, REF_CG_ITERS, nit)
             if step >= args.warmup:
                 vals.append(info['solves_per_s'])
+                step_ms.append(1e3 * (time.perf_counter() - t0))
+        info['value_kind'] = ('scaled from a timed sample: one step = %d CG iterations; a complete solve does not fit '
+                              'the run, so ms_per_step is the sample\'s time, not 1/value' % nit)
         if args.n != 128:
             info['sample'] += ' (Newton and CG counts of the 128^3 workload)'
     v = statistics.median(vals)
-    line = {'impl': 'reference', 'metric': 'RVE solves/s (Newton-CG, %d^3 finite-strain LE1)' % args.n, 'value': v,
+    line = {'impl': 'reference', 'metric': metric_name(args.n), 'value': v,
             'unit': 'solves/s', 'higher_is_better': True, 'n_gpus': args.gpus, 'steps': args.steps,
-            'warmup': args.warmup, 'ms_per_step': 1000.0 / v, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f64',
-            'data': 'synthetic (seeded spheres, seed %d)' % w['seed'],
+            'warmup': args.warmup, 'ms_per_step': statistics.median(step_ms), 'scaling': 'weak', 'vs_baseline': None,
+            'dtype': 'f64', 'data': 'synthetic (seeded spheres, seed %d)' % w['seed'],
             'config': {'workload': 'spheres%d_finite_le1' % args.n, 'resolution': w['res'], 'nb_spheres': 40,
                        'cg_tol': w['cg_tol'], 'newton_tol': w['newton_tol'], 'formulation': 'finite_strain'},
+            'value_kind': info['value_kind'],
             'cpu_baseline': {'value': v, 'unit': 'solves/s', 'cores': info['cores'], 'kind': 'port',
                              'sample': info['sample']},
             'e2e': {'value': v, 'unit': 'solves/s', 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0}}
@@ -457,7 +481,7 @@ def main():
     e2e_v = world / statistics.median(e2e_t)
 
     line = {
-        'metric': 'RVE solves/s (FP32-mixed Newton-CG, %d^3 finite-strain LE1, 40 spheres)' % args.n,
+        'metric': metric_name(args.n),
         'value': value, 'unit': 'solves/s', 'n_gpus': world, 'steps': args.steps, 'warmup': args.warmup,
         'ms_per_step': t_ms / args.steps, 'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None,
         'dtype': 'f32-mixed (f64 Newton)', 'data': 'synthetic (seeded spheres, seed %d)' % w['seed'],
@@ -479,7 +503,7 @@ def main():
     if rank == 0 and world == 1 and not args.no_extra:
         line['configs'] = extra_configs(mu, workloads)
     if rank == 0 and not args.no_cpu:
-        cb = cpu_baseline(w, r64.nb_it, int(round(fp64_cg_per_solve)), args.cpu_cg_iters)
+        cb = cpu_baseline(w, args.cpu_cg_iters)
         line['cpu_baseline'] = {'value': cb['solves_per_s'], 'unit': 'solves/s', 'cores': cb['cores'], 'kind': 'port',
                                 'sample': cb['sample'], 'pxit_per_s': cb['pxit_per_s']}
     if pg:

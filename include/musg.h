@@ -330,8 +330,11 @@ int musg_projection_apply(musg_projection *proj, double *vec);
  * returns before it finishes.  All temporaries live in one 64 MiB file-scope device
  * array that every GPU loading the library holds until exit; grids that do not fit
  * are rejected with MUSG_ERR_ARGUMENT.  The first call on a device looks the
- * array's address up, so make it before any stream capture.  Calls share the
- * array: calls that overlap on the GPU race and must be serialised by the caller. */
+ * array's address up, so make it before any stream capture; under CUDA's lazy
+ * module loading it is also the point where the 64 MiB may be committed, so a
+ * caller that hands the rest of the device to a pool makes one call first (or sets
+ * CUDA_MODULE_LOADING=EAGER).  Calls share the array: calls that overlap on the
+ * GPU race and must be serialised by the caller. */
 int musg_projection_apply_noalloc(int dim, const int *resolutions, const double *lengths,
                                   int kind, int flags, const double *in_device,
                                   double *out_device, void *cuda_stream);

@@ -83,6 +83,15 @@ struct OptimizeResult {
 
 class Cell;
 
+// Communicator (src/common/communicator.hh:107-125, the build without MPI): one rank;
+// a cell runs on one GPU, and independent cells on other GPUs need no exchange
+class Communicator {
+ public:
+  int rank() const { return 0; }
+  int size() const { return 1; }
+  template <typename T> T sum(const T &arg) const { return arg; }
+};
+
 // MaterialBase (material_base.hh:103-150): a handle into the owning cell
 class MaterialBase {
  public:
@@ -128,6 +137,8 @@ class Cell {
     return size_t(n);
   }
   Formulation get_formulation() const { return form_; }
+  // Cell::get_communicator (cell_base.hh:124, 502-503)
+  const Communicator &get_communicator() const { return comm_; }
   std::array<Dim_t, 2> get_strain_shape() const { return {dim_, dim_}; }
   const std::vector<int> &get_domain_resolutions() const { return res_; }
   // CellBase::initialise (cell_base.cc:445-454)
@@ -233,6 +244,7 @@ class Cell {
   std::vector<int> res_;
   std::vector<std::unique_ptr<MaterialBase>> materials_;
   std::map<std::string, std::pair<size_t, std::vector<Real>>> managed_;
+  Communicator comm_;
 };
 
 // CellBase<DimS, DimM> with DimS = DimM = Dim

@@ -14,7 +14,7 @@ there is no CPU fallback.
 """
 from . import batch, fft, material, solvers  # noqa: F401
 from ._lib import ConvergenceError, CudaError, ProjectionError, SolverError, device_count, selftest_wait_timeout  # noqa: F401
-from .cell import (Cell, CellBase, CellBase2d, CellBase3d, CellFactory, FFT_PlanFlags, Formulation,  # noqa: F401
+from .cell import (Cell, CellBase, CellBase2d, CellBase3d, CellFactory, Communicator, FFT_PlanFlags, Formulation,  # noqa: F401
                    SystemFactory, get_domain_ccoord, get_domain_index, get_hermitian_sizes)
 
 __version__ = '0.1.0'

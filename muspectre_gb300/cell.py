@@ -53,6 +53,21 @@ def get_domain_index(sizes: Sequence[int], ccoord: Sequence[int]) -> int:
     return idx
 
 
+class Communicator:
+    """The single-rank communicator (src/common/communicator.hh:107-125, the build
+    without MPI): a cell runs on one GPU; independent cells on other GPUs need no
+    exchange (replicas)."""
+
+    def rank(self):
+        return 0
+
+    def size(self):
+        return 1
+
+    def sum(self, arg):
+        return arg
+
+
 class CellBase:
     """CellBase<D,D> on the GPU (src/cell/cell_base.hh:241-526).
 
@@ -114,6 +129,10 @@ class CellBase:
 
     def get_formulation(self):
         return self.formulation
+
+    def get_communicator(self):
+        """Cell::get_communicator (cell_base.hh:124, 502-503): one rank."""
+        return Communicator()
 
     def get_strain_shape(self):
         return [self.dim, self.dim]

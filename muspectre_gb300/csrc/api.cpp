@@ -667,7 +667,7 @@ struct musg_solver {
       MUSG_CUDA(cudaStreamSynchronize(s));
       if (fault) {
         MUSG_CUDA(cudaMemsetAsync(wait_fault_word(), 0, sizeof fault, s));
-        throw Error(MUSG_ERR_RUNTIME, "a spectral pass timed out waiting for its tile copy (device state unreliable)");
+        throw Error(MUSG_ERR_RUNTIME, "a spectral pass timed out waiting for its tile copy; a copy may still land in shared memory after its block exited, so later results of this CUDA context are suspect: check them or restart the process");
       }
     }
     counter = hst->counter;

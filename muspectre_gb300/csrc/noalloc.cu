@@ -11,9 +11,16 @@
 // routine, on the device or the host.
 //
 // Properties a caller must know:
-//  * The array is part of the library image: every GPU that loads libmusg holds
-//    kNoAllocScratchBytes (64 MiB) for it until the process exits.
-//  * Grids whose temporaries do not fit are rejected with MUSG_ERR_ARGUMENT.
+//  * The array is part of the library image: every GPU that loads libmusg's device
+//    code holds kNoAllocScratchBytes (64 MiB) for it until the process exits.  Under
+//    CUDA's lazy module loading (the default since CUDA 12.2) that memory is
+//    committed when the module is first used on the device, at the latest by the
+//    first call here; if a caller's pool has taken the device memory by then, that
+//    first call fails with MUSG_ERR_CUDA (out of memory).  Callers that reserve the
+//    device memory for a pool should make one call (any small grid) before they do,
+//    or run with CUDA_MODULE_LOADING=EAGER.
+//  * Grids whose temporaries do not fit are rejected with MUSG_ERR_ARGUMENT before
+//    anything is looked up or launched.
 //  * The first call on a device looks the array's device address up
 //    (cudaGetSymbolAddress) and caches it; make that first call before any CUDA
 //    stream capture.
@@ -169,6 +176,14 @@ void noalloc_project(int dim, const int *resolutions, const double *lengths, int
   sp.proj_kind = kind;
   sp.allow_even = allow_even;
   const long long nb_dof = sp.g.npx * sp.ncomp;
+  // the field copy and the half spectrum alone bound every axis length well below
+  // what the FFT plans can factorise, so reject oversized grids before planning
+  const double need0 = (double)nb_dof * sizeof(double) + (double)sp.ncomp * (double)sp.g.nk * sizeof(double2);
+  if (need0 > (double)kNoAllocScratchBytes)
+    throw Error(MUSG_ERR_ARGUMENT, "grid too large for the allocation-free projection: its field copy and half "
+                                   "spectrum alone need " + std::to_string((long long)need0) +
+                                       " bytes of scratch, the maximum is " + std::to_string(kNoAllocScratchBytes) +
+                                       " (64 MiB)");
 
   // layout of the array: [field planes][half spectrum][per axis: tw, chirp, bf, xi]
   size_t off = 0;

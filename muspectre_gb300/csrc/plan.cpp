@@ -89,6 +89,7 @@ void AxisPlan::build(int n_) {
     m = n;
   } else {
     blu = 1;
+    if (n > (1 << 28)) throw Error(MUSG_ERR_ARGUMENT, "FFT length too large");
     m = smooth_at_least(2 * n - 1);
     factorize(m, rad);
   }

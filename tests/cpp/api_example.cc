@@ -24,6 +24,11 @@ int main(int argc, char **argv) {
     return 0;
   }
   auto rve = make_cell<2>({51, 51}, {7., 5.}, Formulation::small_strain);
+  const Communicator &comm = rve->get_communicator();  // single rank, as without MPI
+  if (comm.rank() != 0 || comm.size() != 1 || comm.sum(2.5) != 2.5) {
+    std::puts("unexpected communicator");
+    return 1;
+  }
   auto &hard = MaterialLinearElastic1<2>::make(*rve, "hard", 10e9, .33);
   auto &soft = MaterialLinearElastic1<2>::make(*rve, "soft", 70e9, .33);
   for (size_t i = 0; i < rve->size(); ++i) {

@@ -13,7 +13,7 @@ copied into this repository):
   to ``float`` so that it runs on NumPy 2) to write Ĝ and projection results at 5² and
   5³ for the small- and finite-strain operators.
 
-Usage:  python tests/golden/make_golden.py /root/reference
+Usage:  python tests/golden/make_golden.py <path of the reference source tree>
 Writes ``tests/golden/hep1_kat.json``, ``expm_kat.json``, ``fftfreq_kat.json`` and
 ``goose_projection.npz`` next to this script.
 """
@@ -119,4 +119,6 @@ def main(ref):
 
 
 if __name__ == '__main__':
-    main(sys.argv[1] if len(sys.argv) > 1 else '/root/reference')
+    if len(sys.argv) != 2:
+        sys.exit('usage: make_golden.py <path of the reference source tree>')
+    main(sys.argv[1])

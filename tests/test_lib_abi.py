@@ -68,4 +68,8 @@ def test_python_api_surface():
             assert hasattr(mu.fft, '%s_%dd' % (p, d))
     assert hasattr(mu.solvers, 'SolverCG') and hasattr(mu.solvers, 'newton_cg')
     assert mu.get_hermitian_sizes([6, 4]) == [6, 3]
+    # Cell::get_communicator: the single-rank stub (communicator.hh:107-125)
+    comm = mu.Communicator()
+    assert (comm.rank(), comm.size(), comm.sum(2.5)) == (0, 1, 2.5)
+    assert hasattr(mu.CellBase, 'get_communicator')
     assert mu.get_domain_index([3, 4, 5], mu.get_domain_ccoord([3, 4, 5], 37)) == 37

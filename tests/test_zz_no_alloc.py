@@ -5,8 +5,10 @@ library -- a caller-owned pool or arena that forbids cudaMalloc, or an
 allocation-free real-time loop -- and hand in their own device buffers.  This test
 calls it through the C ABI on device buffers, twice in a row for every case, and
 compares it with the allocating musg_projection_apply at the projection tests'
-tolerance (1e-13 relative).  It also checks that a grid too large for the fixed
-scratch array is rejected with a clear error.  The file is collected last.
+tolerance (1e-13 relative).  On the second call of every case the device's free
+memory (cudaMemGetInfo) is read right before and after the call and must not
+change: the call allocates nothing.  It also checks that a grid too large for the
+fixed scratch array is rejected with a clear error.  The file is collected last.
 """
 import ctypes as C
 
@@ -51,10 +53,15 @@ def test_noalloc_projection_matches_allocating_entry_point():
             # the allocation-free one on device buffers
             d_in = torch.from_numpy(f).to('cuda')
             d_out = torch.full_like(d_in, float('nan'))
+            torch.cuda.synchronize()
+            free0 = torch.cuda.mem_get_info()[0]
             L.check(lib.musg_projection_apply_noalloc(dim, L.iptr(r), L.dptr(ln), kind, flags,
                                                       C.c_void_p(d_in.data_ptr()), C.c_void_p(d_out.data_ptr()),
                                                       C.c_void_p(stream.cuda_stream)))
             stream.synchronize()
+            free1 = torch.cuda.mem_get_info()[0]
+            if call == 1:
+                assert free1 == free0, ('device memory changed across the call', res, free0, free1)
             got = d_out.cpu().numpy()
             assert np.all(np.isfinite(got))
             assert rel(got, ref) < 1e-13, (call, res)
