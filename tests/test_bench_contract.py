@@ -23,3 +23,42 @@ def test_reference_arm_line():
     assert cb['kind'] == 'port' and cb['cores'] >= 1 and 'complete solves' in cb['sample'] and cb['value'] == line['value']
     e2e = line['e2e']
     assert e2e['value'] == line['value'] and e2e['h2d_bytes_per_step'] == 0 and e2e['d2h_bytes_per_step'] == 0
+
+
+def test_reference_arm_metric_matches_ours():
+    """Both arms print one metric string, so that their values can be divided."""
+    sys.path.insert(0, ROOT)
+    import bench
+    assert bench.metric_name(128) == 'RVE solves/s (Newton-CG, 128^3 finite-strain LE1, 40 spheres)'
+    src = open(os.path.join(ROOT, 'bench.py')).read()
+    assert src.count("'metric': metric_name(args.n)") == 2
+
+
+def test_scaled_sample_matches_complete_solves():
+    """The reference arm's method at 128^3 (no complete solve fits the run): the
+    Newton-level work timed once plus a timed sample of 8 CG iterations, scaled by the
+    Newton and CG counts of a complete solve.  At 32^3 and 48^3, where a complete
+    oracle solve takes seconds, the scaled estimate of the solve time is within 25%
+    of the timed complete solve (measured: within 4%)."""
+    import time
+    sys.path.insert(0, ROOT)
+    import bench
+    from muspectre_gb300 import workloads
+    from oracle import muspectre_oracle as o
+    saved = o.FFT_WORKERS
+    o.FFT_WORKERS = os.cpu_count() or 1
+    try:
+        for n in (32, 48):
+            w = workloads.spheres(n)
+            t0 = time.perf_counter()
+            oc = workloads.build_spheres_oracle(o, w)
+            r = o.newton_cg(oc, w['load'], o.SolverCG(oc, w['cg_tol'], w['maxiter']), w['newton_tol'],
+                            w['equil_tol'], 0)
+            t_full = time.perf_counter() - t0
+            smp = bench.CpuSample(w)
+            est = smp.describe(smp.cg_iteration_seconds(bench.REF_SAMPLE_CG_ITERS), r.nb_it, r.nb_fev,
+                               bench.REF_SAMPLE_CG_ITERS)
+            ratio = t_full * est['solves_per_s']
+            assert 0.75 < ratio < 1.25, (n, t_full, 1.0 / est['solves_per_s'])
+    finally:
+        o.FFT_WORKERS = saved
