@@ -55,7 +55,10 @@ extern "C" {
 #define MUSG_LAW_LE2 2  /* MaterialLinearElastic2:  params (E, nu); per pixel D*D eigenstrain */
 #define MUSG_LAW_LE3 3  /* MaterialLinearElastic3:  per pixel (E, nu), full C   */
 #define MUSG_LAW_LE4 4  /* MaterialLinearElastic4:  per pixel (E, nu) -> (lambda, mu) */
-#define MUSG_LAW_HEP1 5 /* MaterialHyperElastoPlastic1: params (E, nu, tau_y0, H) */
+#define MUSG_LAW_HEP1 5 /* MaterialHyperElastoPlastic1: params (E, nu, tau_y0, H[, mode]);
+                           mode 0 the reference (projector logm, j-independent Kirchhoff->PK1
+                           tangent), 1 spectral logm, 2 spectral logm with the consistent
+                           tangent dP/dF and eps_p.cur = eps_p.old + dgamma (extensions) */
 #define MUSG_LAW_GENERIC 6 /* MaterialLinearElasticGeneric: params the Voigt stiffness,
                               vsize x vsize row-major (vsize 3 in 2-D, 6 in 3-D) */
 
@@ -78,6 +81,9 @@ typedef struct musg_result_info {
   unsigned nb_it;        /* Newton iterations of this load step        */
   unsigned nb_fev;       /* cumulative CG iterations (solver counter)  */
   char message[64];      /* OptimizeResult::message                    */
+  double hom_stress[9];  /* pixel mean of the stress after the load step, D*D column-major
+                            (no counterpart: the reference's callers average
+                            OptimizeResult::stress themselves, solvers.cc:197) */
 } musg_result_info;
 
 /* -------------------------------------------------------------- library */
@@ -183,6 +189,12 @@ int musg_solver_destroy(musg_solver *solver);
  * solve stops at max(tol, inner_tol), default 1e-2 (the forcing term of an inexact
  * Newton method), and newton_cg refines in FP64 */
 int musg_solver_set_inner_tol(musg_solver *solver, double inner_tol);
+/* newton_cg with a backtracking line search (no counterpart in the reference; off by
+ * default): every Newton increment dF is applied as F0 + lam dF with lam = 1, 1/2, ...
+ * until the norm of the projected residual G(-P) falls below (1 - 1e-4 lam) of the
+ * current one, or lam = 1/1024; the convergence test still measures |dF|.  It lets the
+ * consistent elasto-plastic tangent (HEP1 mode 2) converge on heterogeneous cells. */
+int musg_solver_set_line_search(musg_solver *solver, int enable);
 /* SolverBase::get_counter / reset_counter / has_converged (solver_base.hh:62-109) */
 int musg_solver_get_counter(musg_solver *solver, unsigned *counter);
 int musg_solver_reset_counter(musg_solver *solver);

@@ -340,14 +340,17 @@ template <int Dim> class MaterialLinearElasticGeneric : public MaterialBase {
   void add_pixels(const std::vector<long long> &idx) { add(idx, {}, 0); }
 };
 
-// MaterialHyperElastoPlastic1 (material_hyper_elasto_plastic1.cc:41-65)
+// MaterialHyperElastoPlastic1 (material_hyper_elasto_plastic1.cc:41-65); mode 0 is the
+// reference, 1 the spectral logm, 2 the spectral logm with the consistent tangent
+// (extensions, see MUSG_LAW_HEP1)
 template <int Dim> class MaterialHyperElastoPlastic1 : public MaterialBase {
  public:
-  MaterialHyperElastoPlastic1(Cell &c, const std::string &name, Real young, Real poisson, Real tau_y0, Real H)
-      : MaterialBase(c, MUSG_LAW_HEP1, name, {young, poisson, tau_y0, H, 0.0}) {}
+  MaterialHyperElastoPlastic1(Cell &c, const std::string &name, Real young, Real poisson, Real tau_y0, Real H,
+                              int mode = 0)
+      : MaterialBase(c, MUSG_LAW_HEP1, name, {young, poisson, tau_y0, H, Real(mode)}) {}
   static MaterialHyperElastoPlastic1 &make(CellBase<Dim> &cell, const std::string &name, Real young, Real poisson,
-                                          Real tau_y0, Real H) {
-    return cell.adopt(std::make_unique<MaterialHyperElastoPlastic1>(cell, name, young, poisson, tau_y0, H));
+                                          Real tau_y0, Real H, int mode = 0) {
+    return cell.adopt(std::make_unique<MaterialHyperElastoPlastic1>(cell, name, young, poisson, tau_y0, H, mode));
   }
   void add_pixel(const std::array<int, Dim> &c) { add({index_of(c.data())}, {}, 0); }
 };
@@ -383,6 +386,8 @@ class SolverCG {
     return c != 0;
   }
   void set_inner_tol(Real t) { check(musg_solver_set_inner_tol(h_, t)); }
+  // newton_cg with a backtracking line search (extension; see musg_solver_set_line_search)
+  void set_line_search(bool on) { check(musg_solver_set_line_search(h_, on ? 1 : 0)); }
   // SolverCG::solve: x = A^-1 rhs
   std::vector<Real> solve(const std::vector<Real> &rhs) {
     std::vector<Real> x(rhs.size());

@@ -41,7 +41,7 @@ class CudaError(RuntimeError):
 
 class ResultInfo(C.Structure):
     _fields_ = [('success', C.c_int), ('status', C.c_int), ('nb_it', C.c_uint), ('nb_fev', C.c_uint),
-                ('message', C.c_char * 64)]
+                ('message', C.c_char * 64), ('hom_stress', C.c_double * 9)]
 
 
 class Request(C.Structure):
@@ -100,6 +100,7 @@ _SIGNATURES = {
     'musg_solver_cg_create': (C.c_int, [_P, C.c_double, C.c_uint, C.c_int, C.c_int, C.POINTER(_P)]),
     'musg_solver_destroy': (C.c_int, [_P]),
     'musg_solver_set_inner_tol': (C.c_int, [_P, C.c_double]),
+    'musg_solver_set_line_search': (C.c_int, [_P, C.c_int]),
     'musg_solver_get_counter': (C.c_int, [_P, C.POINTER(C.c_uint)]),
     'musg_solver_reset_counter': (C.c_int, [_P]),
     'musg_solver_has_converged': (C.c_int, [_P, _I]),

@@ -74,7 +74,7 @@ class BatchSolver:
                 rs.append(OptimizeResult(np.empty((0, 1)),
                                          stresses[b, k].reshape(-1, 1) if return_stress else np.empty((0, 1)),
                                          bool(i.success), int(i.status), i.message.decode(), int(i.nb_it),
-                                         int(i.nb_fev)))
+                                         int(i.nb_fev), np.array(i.hom_stress[:d * d]).reshape(d, d).T))
             self.cells[b]._has_tangent = True
             out.append(rs)
         return out

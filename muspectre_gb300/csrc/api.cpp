@@ -170,13 +170,14 @@ struct musg_cell {
   template <typename R> int tk() const { return sizeof(R) == 4 ? tkind32 : tkind; }
   int hep_cur = 0;
   bool has_le2 = false, has_hep = false;
+  bool has_consistent = false;  // an HEP1 material with the consistent tangent: TK_FULL cell
   // device fields (FP64 component planes)
-  DevBuf F, P, rhs, io, io2;
+  DevBuf F, P, rhs, io, io2, F0;  // F0: the line search's Newton iterate
   DevBuf mat, params, law_kind, Ctab64, Ctab32;
   bool has_generic = false;
   DevBuf lam64, mu64, lam32, mu32, eig;
   DevBuf Fprev[2], be[2], eps[2];
-  DevBuf S64, S32, Kp64, Kp32, Fc64, Fc32, Kfull;
+  DevBuf S64, S32, Kp64, Kp32, Fc64, Fc32, Kfull, Kt64, Kt32;
   DevBuf partial, scal;  // reduction scratch, small device scalars
   DevBuf nonfinite;
   double *hscal = nullptr;  // pinned host mirror of scal
@@ -288,6 +289,7 @@ struct musg_cell {
       q.H = mt.H;
       if (mt.law == MUSG_LAW_HEP1) {
         has_hep = true;
+        has_consistent |= mt.logm_mode == kHep1Consistent;
         hkind[m] = TK_KPRIME;
       } else {
         any_le = true;
@@ -311,6 +313,7 @@ struct musg_cell {
     require(!(has_hep && form == MUSG_SMALL_STRAIN), MUSG_ERR_ARGUMENT,
             "MaterialHyperElastoPlastic1 needs the finite-strain formulation");
     if (form == MUSG_SMALL_STRAIN) tkind = TK_SMALL;
+    else if (has_consistent) tkind = TK_FULL;  // every pixel's dP/dF stored (D^4 planes)
     else if (has_hep && any_le) tkind = TK_MIXED;
     else if (has_hep) tkind = TK_KPRIME;
     else tkind = TK_FINITE;
@@ -379,7 +382,8 @@ struct musg_cell {
       fill_uniform(Fprev[0].as<double>(), Id, D2, npx, stream);
       fill_uniform(be[0].as<double>(), Id, D2, npx, stream);
       hep_cur = 1;
-      Kp64.alloc((size_t)npx * D2 * dim * sizeof(double));
+      if (tkind == TK_FULL) Kt64.alloc((size_t)npx * D2 * D2 * sizeof(double));
+      else Kp64.alloc((size_t)npx * D2 * dim * sizeof(double));
     }
     if (need32) alloc32();
     initialised = true;
@@ -414,7 +418,8 @@ struct musg_cell {
     if (form == MUSG_FINITE_STRAIN) {
       if (!S32.p) S32.alloc((size_t)nb_dof() * sizeof(float));
       if (!Fc32.p) Fc32.alloc((size_t)nb_dof() * sizeof(float));
-      if (has_hep && !Kp32.p) Kp32.alloc((size_t)npx * D2 * dim * sizeof(float));
+      if (has_hep && tkind != TK_FULL && !Kp32.p) Kp32.alloc((size_t)npx * D2 * dim * sizeof(float));
+      if (tkind == TK_FULL && !Kt32.p) Kt32.alloc((size_t)npx * D2 * D2 * sizeof(float));
     }
     tangent_valid = false;
     autotune();
@@ -444,6 +449,8 @@ struct musg_cell {
     a.Kp64 = Kp64.as<double>();
     a.S32 = tkind32 == TK_FISO ? nullptr : S32.as<float>();
     a.Kp32 = Kp32.as<float>();
+    a.Kt64 = Kt64.as<double>();
+    a.Kt32 = Kt32.as<float>();
     a.Fc32 = Fc32.as<float>();
     a.Fc64 = Fc64.as<double>();
     if (want_K) {
@@ -461,6 +468,16 @@ struct musg_cell {
   void save_history() {
     // StateField::cycle (statefield.hh:322-326): swap current and old
     if (has_hep) hep_cur = 1 - hep_cur;
+  }
+
+  // the pixel mean of the stress field (D*D column-major) into out (host, 9 entries),
+  // reduced on the device in a fixed order
+  void homogenised(double *out) {
+    double *d = scal.as<double>() + 40;
+    plane_means(P.as<double>(), D2, npx, partial.as<double>(), d, stream);
+    MUSG_CUDA(cudaMemcpyAsync(hscal + 40, d, D2 * sizeof(double), cudaMemcpyDeviceToHost, stream));
+    MUSG_CUDA(cudaStreamSynchronize(stream));
+    for (int k = 0; k < 9; ++k) out[k] = k < D2 ? hscal[40 + k] : 0.0;
   }
 
   // host AoS vector -> device SoA planes (dst)
@@ -484,6 +501,7 @@ template <> TangentData<double> musg_cell::tangent<double>() const {
   t.F = Fc64.as<double>();
   t.S = S64.as<double>();
   t.Kp = Kp64.as<double>();
+  t.Kt = Kt64.as<double>();
   t.mat = mat.as<uint8_t>();
   t.law_kind = law_kind.as<uint8_t>();
   t.C = Ctab64.as<double>();
@@ -497,6 +515,7 @@ template <> TangentData<float> musg_cell::tangent<float>() const {
   t.F = Fc32.as<float>();
   t.S = S32.as<float>();
   t.Kp = Kp32.as<float>();
+  t.Kt = Kt32.as<float>();
   t.mat = mat.as<uint8_t>();
   t.law_kind = law_kind.as<uint8_t>();
   t.C = Ctab32.as<float>();
@@ -524,6 +543,9 @@ struct musg_solver {
   // inner solve costs fewer CG iterations in total (FP32 CG could not go much below
   // ~1e-6 on stiff-contrast cells anyway)
   double inner_tol = 1e-2;
+  // newton_cg with a backtracking line search on the projected residual norm (an
+  // extension, off by default; needed by the consistent elasto-plastic tangent)
+  bool line_search = false;
 
   ~musg_solver() {
     if (exec) cudaGraphExecDestroy(exec);
@@ -893,29 +915,58 @@ void newton_cg_impl(musg_cell *cell, const double *steps, int nsteps, musg_solve
       return has_converged;
     };
     unsigned newt_iter = 0;
+    bool evaluated = false;  // a line-search trial left P and rhs at the current F
     for (; newt_iter < solver->maxiter && !has_converged; ++newt_iter) {
-      c.evaluate(false);
       const bool first_geus = geus && newt_iter == 0;
-      if (first_geus) {
-        // rhs = -G(K:DF) with DF the uniform macroscopic increment (FP64)
-        fill_uniform(c.rhs.as<double>(), ddelta, D2, c.npx, s);
-        tangent_operator<double>(c.sp, c.tkind, c.tangent<double>(), c.rhs.as<double>(), c.rhs.as<double>(), s);
-        convert<double, double>(c.rhs.as<double>(), c.rhs.as<double>(), n, -1.0, s);
+      if (evaluated) {
+        evaluated = false;
       } else {
-        // rhs = -P, projected (FP64)
-        spectral_project<double>(c.sp, c.P.as<double>(), c.rhs.as<double>(), -1.0, s);
+        c.evaluate(false);
+        if (first_geus) {
+          // rhs = -G(K:DF) with DF the uniform macroscopic increment (FP64)
+          fill_uniform(c.rhs.as<double>(), ddelta, D2, c.npx, s);
+          tangent_operator<double>(c.sp, c.tkind, c.tangent<double>(), c.rhs.as<double>(), c.rhs.as<double>(), s);
+          convert<double, double>(c.rhs.as<double>(), c.rhs.as<double>(), n, -1.0, s);
+        } else {
+          // rhs = -P, projected (FP64)
+          spectral_project<double>(c.sp, c.P.as<double>(), c.rhs.as<double>(), -1.0, s);
+        }
+        dot_device<double, double>(c.rhs.as<double>(), c.rhs.as<double>(), n, c.partial.as<double>(), dscal + 32, s);
+        MUSG_CUDA(cudaMemcpyAsync(c.hscal + 32, dscal + 32, sizeof(double), cudaMemcpyDeviceToHost, s));
+        MUSG_CUDA(cudaStreamSynchronize(s));
+        stress_norm = std::sqrt(c.hscal[32]);
       }
-      dot_device<double, double>(c.rhs.as<double>(), c.rhs.as<double>(), n, c.partial.as<double>(), dscal + 32, s);
-      MUSG_CUDA(cudaMemcpyAsync(c.hscal + 32, dscal + 32, sizeof(double), cudaMemcpyDeviceToHost, s));
-      MUSG_CUDA(cudaStreamSynchronize(s));
-      stress_norm = std::sqrt(c.hscal[32]);
       if (convergence_test()) break;
       solver->solve_device_any(c.rhs.as<double>());
       if (first_geus) add_macro(c.F.as<double>(), ddelta, D2, c.npx, s);
-      if (solver->precision == MUSG_PRECISION_MIXED)
+      if (solver->line_search && !first_geus) {
+        // F = F0 + lam dF for lam = 1, 1/2, ... until the projected residual norm drops
+        // below (1 - 1e-4 lam) of the current one (Armijo), or lam = 1/1024; the
+        // accepted trial's evaluation serves the next Newton iteration
+        if (c.F0.bytes < c.field_bytes()) c.F0.alloc(c.field_bytes());
+        MUSG_CUDA(cudaMemcpyAsync(c.F0.p, c.F.p, c.field_bytes(), cudaMemcpyDeviceToDevice, s));
+        const double nr = stress_norm;
+        for (double lam = 1.0;; lam *= 0.5) {
+          if (solver->precision == MUSG_PRECISION_MIXED)
+            newton_trial<float>(c.F.as<double>(), c.F0.as<double>(), solver->x.as<float>(), lam, n,
+                                c.partial.as<double>(), dscal + 34, s);
+          else
+            newton_trial<double>(c.F.as<double>(), c.F0.as<double>(), solver->x.as<double>(), lam, n,
+                                 c.partial.as<double>(), dscal + 34, s);
+          c.evaluate(false);
+          spectral_project<double>(c.sp, c.P.as<double>(), c.rhs.as<double>(), -1.0, s);
+          dot_device<double, double>(c.rhs.as<double>(), c.rhs.as<double>(), n, c.partial.as<double>(), dscal + 32, s);
+          MUSG_CUDA(cudaMemcpyAsync(c.hscal + 32, dscal + 32, 4 * sizeof(double), cudaMemcpyDeviceToHost, s));
+          MUSG_CUDA(cudaStreamSynchronize(s));
+          stress_norm = std::sqrt(c.hscal[32]);
+          if (stress_norm < (1.0 - 1e-4 * lam) * nr || lam <= 1.0 / 1024) break;
+        }
+        evaluated = true;
+      } else if (solver->precision == MUSG_PRECISION_MIXED) {
         newton_update<float>(c.F.as<double>(), solver->x.as<float>(), n, c.partial.as<double>(), dscal + 34, s);
-      else
+      } else {
         newton_update<double>(c.F.as<double>(), solver->x.as<double>(), n, c.partial.as<double>(), dscal + 34, s);
+      }
       MUSG_CUDA(cudaMemcpyAsync(c.hscal + 34, dscal + 34, 2 * sizeof(double), cudaMemcpyDeviceToHost, s));
       MUSG_CUDA(cudaStreamSynchronize(s));
       incr_norm = std::sqrt(c.hscal[34]);
@@ -940,6 +991,7 @@ void newton_cg_impl(musg_cell *cell, const double *steps, int nsteps, musg_solve
       ri.nb_fev = (unsigned)solver->counter;
       memset(ri.message, 0, sizeof(ri.message));
       strncpy(ri.message, message.c_str(), sizeof(ri.message) - 1);
+      c.homogenised(ri.hom_stress);
     }
     if (grads) c.download_field(c.F.as<double>(), grads + (size_t)step * n);
     if (stresses) c.download_field(c.P.as<double>(), stresses + (size_t)step * n);
@@ -1073,6 +1125,8 @@ void batch_newton_impl(musg_batch *batch, const double *steps, int nsteps, doubl
       ri.nb_fev = (unsigned)bt.solvers[b]->counter;
       memset(ri.message, 0, sizeof(ri.message));
       strncpy(ri.message, failed[b] ? errmsg[b].c_str() : message[b].c_str(), sizeof(ri.message) - 1);
+      if (!failed[b]) c.homogenised(ri.hom_stress);
+      else std::fill(ri.hom_stress, ri.hom_stress + 9, std::nan(""));
       if (stresses && !failed[b]) c.download_field(c.P.as<double>(), stresses + ((size_t)b * nsteps + step) * n);
       if (!failed[b]) c.save_history();
     }
@@ -1217,6 +1271,8 @@ int musg_material_create(musg_cell *cell, int law, const char *name, const doubl
         m.tau_y0 = params[2];
         m.H = params[3];
         m.logm_mode = nb_params >= 5 ? (int)params[4] : 0;
+        require(m.logm_mode >= 0 && m.logm_mode <= kHep1Consistent, MUSG_ERR_ARGUMENT,
+                "HEP1 mode: 0 projector logm, 1 spectral logm, 2 spectral logm with the consistent tangent");
         break;
       default:
         throw Error(MUSG_ERR_ARGUMENT, "unknown material law");
@@ -1552,6 +1608,13 @@ int musg_solver_cg_create(musg_cell *cell, double tol, unsigned maxiter, int ver
     auto s = std::make_unique<musg_solver>();
     s->create(cell, tol, maxiter, verbose, precision);
     *out = s.release();
+  });
+}
+
+int musg_solver_set_line_search(musg_solver *solver, int enable) {
+  return guard([&] {
+    require(solver, MUSG_ERR_ARGUMENT, "null solver");
+    solver->line_search = enable != 0;
   });
 }
 

@@ -218,6 +218,26 @@ __global__ void k_newton_update(double *__restrict__ F, const R *__restrict__ x,
   if (threadIdx.x == 0) partial[nparts + blockIdx.x] = s2;
 }
 
+// line-search trial F = F0 + lam x; partial sums of x.x (the full Newton increment)
+// and F.F
+template <typename R>
+__global__ void k_newton_trial(double *__restrict__ F, const double *__restrict__ F0, const R *__restrict__ x,
+                               double lam, long long n, double *partial, int nparts) {
+  double axx = 0.0, aff = 0.0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const double xv = (double)x[i];
+    const double f = F0[i] + lam * xv;
+    F[i] = f;
+    axx += xv * xv;
+    aff += f * f;
+  }
+  const double s1 = block_sum(axx);
+  if (threadIdx.x == 0) partial[blockIdx.x] = s1;
+  __syncthreads();
+  const double s2 = block_sum(aff);
+  if (threadIdx.x == 0) partial[nparts + blockIdx.x] = s2;
+}
+
 __global__ void k_sum2_to(const double *partial, int nparts, double *out) {
   const double a = sum_partials(partial, nparts);
   __syncthreads();
@@ -232,6 +252,16 @@ template <typename R>
 void newton_update(double *F, const R *x, long long n, double *partial, double *out, cudaStream_t s) {
   const int nb = reduce_blocks(n);
   k_newton_update<R><<<nb, kRedThreads, 0, s>>>(F, x, n, partial, nb);
+  MUSG_CHECK_LAUNCH();
+  k_sum2_to<<<1, 1024, 0, s>>>(partial, nb, out);
+  MUSG_CHECK_LAUNCH();
+}
+
+template <typename R>
+void newton_trial(double *F, const double *F0, const R *x, double lam, long long n, double *partial, double *out,
+                  cudaStream_t s) {
+  const int nb = reduce_blocks(n);
+  k_newton_trial<R><<<nb, kRedThreads, 0, s>>>(F, F0, x, lam, n, partial, nb);
   MUSG_CHECK_LAUNCH();
   k_sum2_to<<<1, 1024, 0, s>>>(partial, nb, out);
   MUSG_CHECK_LAUNCH();
@@ -285,6 +315,10 @@ template void dot_device<double, double>(const double *, const double *, long lo
 template void dot_device<float, float>(const float *, const float *, long long, double *, double *, cudaStream_t);
 template void newton_update<double>(double *, const double *, long long, double *, double *, cudaStream_t);
 template void newton_update<float>(double *, const float *, long long, double *, double *, cudaStream_t);
+template void newton_trial<double>(double *, const double *, const double *, double, long long, double *, double *,
+                                   cudaStream_t);
+template void newton_trial<float>(double *, const double *, const float *, double, long long, double *, double *,
+                                  cudaStream_t);
 template void convert<double, double>(double *, const double *, long long, double, cudaStream_t);
 template void convert<float, double>(float *, const double *, long long, double, cudaStream_t);
 template void convert<double, float>(double *, const float *, long long, double, cudaStream_t);

@@ -183,11 +183,8 @@ template <int D> __device__ __forceinline__ M<D> logm_projector(const M<D> &T) {
   return out;
 }
 
-// log(T) = V diag(log w) V^T (defined for repeated eigenvalues; opt-in)
-template <int D> __device__ __forceinline__ M<D> logm_spectral(const M<D> &T) {
-  double w[D];
-  M<D> V;
-  sym_eig<D>(T, w, V);
+// log(T) = V diag(log w) V^T from an eigen-decomposition T = V diag(w) V^T
+template <int D> __device__ __forceinline__ M<D> log_from_eig(const double *w, const M<D> &V) {
   M<D> out;
 #pragma unroll
   for (int j = 0; j < D; ++j)
@@ -199,6 +196,14 @@ template <int D> __device__ __forceinline__ M<D> logm_spectral(const M<D> &T) {
       out(i, j) = v;
     }
   return out;
+}
+
+// first divided difference of log at eigenvalues a, b: (log a - log b) / (a - b), and
+// 1/b at a = b; log1p keeps it accurate when a and b are close (Daleckii-Krein
+// derivative of the matrix logarithm in its eigenbasis)
+__device__ __forceinline__ double log_divdiff(double a, double b) {
+  const double x = (a - b) / b;
+  return x == 0.0 ? 1.0 / b : log1p(x) / (a - b);
 }
 
 // exp(T) = sum_i e^{w_i} v_i v_i^T  (src/common/eigen_tools.hh:329-341)
@@ -221,6 +226,14 @@ template <int D> __device__ __forceinline__ M<D> expm_sym(const M<D> &T) {
 }
 
 template <typename R> __device__ __forceinline__ void store(R *p, long long o, double v) { p[o] = (R)v; }
+
+// one entry (index c + D^2 q of the T4 layout) of a pixel's full tangent into the API's
+// AoS array and the CG operator's planes (TK_FULL), whichever are set
+__device__ __forceinline__ void put_tangent(const MaterialArgs &a, long long px, int d4, int idx, double v) {
+  if (a.Kfull) a.Kfull[px * d4 + idx] = v;
+  if (a.Kt64) a.Kt64[(long long)idx * a.npx + px] = v;
+  if (a.Kt32) a.Kt32[(long long)idx * a.npx + px] = (float)v;
+}
 
 // HEP: the cell has MaterialHyperElastoPlastic1 pixels.  Without them the elasto-plastic
 // branch (eigen-solves, logm/expm) is compiled out, which keeps the elastic laws at a
@@ -291,8 +304,7 @@ __global__ void __launch_bounds__(kMatThreads) k_material(const MaterialArgs a, 
     } else {
       P = S;
     }
-    if (a.Kfull) {
-      double *K = a.Kfull + px * (long long)(D2 * D2);
+    if (a.Kfull || a.Kt64 || a.Kt32) {
 #pragma unroll
       for (int l = 0; l < D; ++l)
 #pragma unroll
@@ -323,7 +335,7 @@ __global__ void __launch_bounds__(kMatThreads) k_material(const MaterialArgs a, 
               } else {
                 v = lam * (i == j && k == l ? 1.0 : 0.0) + mu * ((i == k && j == l ? 1.0 : 0.0) + (i == l && j == k ? 1.0 : 0.0));
               }
-              K[(i + D * j) + D2 * (k + D * l)] = v;
+              put_tangent(a, px, D2 * D2, (i + D * j) + D2 * (k + D * l), v);
             }
     }
   } else {
@@ -336,9 +348,19 @@ __global__ void __launch_bounds__(kMatThreads) k_material(const MaterialArgs a, 
       be.a[c] = a.be[old][c * N + px];
     }
     const double eps_old = a.eps[old][px];
-    const M<D> f = mul<D>(F, inv(Fp));
+    const M<D> Fpi = inv(Fp);
+    const M<D> f = mul<D>(F, Fpi);
     const M<D> be_star = mul_bt<D>(mul<D>(f, be), f);
-    M<D> ln_be = (mp.logm_mode == 0) ? logm_projector<D>(be_star) : logm_spectral<D>(be_star);
+    const bool consistent = mp.logm_mode == kHep1Consistent;
+    double w[D];
+    M<D> V;
+    M<D> ln_be;
+    if (mp.logm_mode == 0) {
+      ln_be = logm_projector<D>(be_star);
+    } else {
+      sym_eig<D>(be_star, w, V);  // kept for the consistent tangent
+      ln_be = log_from_eig<D>(w, V);
+    }
     const double lam = mp.lam, mu = mp.mu;
     M<D> tau_star;
     const double trl = trace<D>(ln_be);
@@ -375,7 +397,10 @@ __global__ void __launch_bounds__(kMatThreads) k_material(const MaterialArgs a, 
       a.Fprev[cur][c * N + px] = F.a[c];
       a.be[cur][c * N + px] = be_new.a[c];
     }
-    a.eps[cur][px] += dgamma;
+    // the reference adds dgamma to the current buffer's stale contents on every
+    // evaluation (...plastic1.hh:262); the consistent mode writes eps_old + dgamma, so
+    // that a repeated evaluation (a line-search trial) leaves the same state
+    a.eps[cur][px] = consistent ? eps_old + dgamma : a.eps[cur][px] + dgamma;
     // material tangent C = alpha Itrac + beta Isymm + gamma N (x) N
     double al, bt, gm;
     if (phi > 0.0) {
@@ -393,6 +418,62 @@ __global__ void __launch_bounds__(kMatThreads) k_material(const MaterialArgs a, 
     // K'(i,m,n) = sum_r Finv(i,r) sum_s C(r,m,n,s)
     const M<D> Fi = inv(F);
     P = mul_bt<D>(tau, Fi);
+    if (consistent) {
+      // The consistent tangent (opt-in; the reference converts with the j-independent
+      // K' below): K(i,m,j,n) = dP(i,m)/dF(j,n) with P = tau F^-T, so
+      //   dP = dtau F^-T - P dF^T F^-T,   i.e. the second term is -P(i,n) Finv(m,j);
+      //   dtau = C : d ln(be*)  (C as above, the derivative of tau in ln be*);
+      //   d ln(be*) = V [g o (V^T dbe* V)] V^T with g(p,q) = log_divdiff(w_p, w_q);
+      //   dbe* = dF Mb + (dF Mb)^T, Mb = F_prev^-1 be_old f^T (be* = f be_old f^T, f = F F_prev^-1).
+      // Column (j, n) is the response to dF = e_j e_n^T.
+      const M<D> Mb = mul_bt<D>(mul<D>(Fpi, be), f);
+      const M<D> MV = mul<D>(Mb, V);
+      M<D> Gd, Nt;
+#pragma unroll
+      for (int q = 0; q < D; ++q)
+#pragma unroll
+        for (int p = 0; p < D; ++p) {
+          Gd(p, q) = p == q ? 1.0 / w[p] : log_divdiff(w[p], w[q]);
+          double v = 0.0;
+#pragma unroll
+          for (int b = 0; b < D; ++b)
+#pragma unroll
+            for (int c2 = 0; c2 < D; ++c2) v += V(b, p) * Nst(b, c2) * V(c2, q);
+          Nt(p, q) = v;
+        }
+#pragma unroll 1
+      for (int n = 0; n < D; ++n)
+#pragma unroll 1
+        for (int j = 0; j < D; ++j) {
+          M<D> sm;
+          double trs = 0.0, nsv = 0.0;
+#pragma unroll
+          for (int q = 0; q < D; ++q)
+#pragma unroll
+            for (int p = 0; p < D; ++p) {
+              const double t = V(j, p) * MV(n, q) + MV(n, p) * V(j, q);
+              const double sv = Gd(p, q) * t;
+              sm(p, q) = sv;
+              nsv += Nt(p, q) * sv;
+              if (p == q) trs += sv;
+            }
+          const M<D> dl = mul_bt<D>(mul<D>(V, sm), V);
+          M<D> dtau;
+#pragma unroll
+          for (int k = 0; k < D2; ++k) dtau.a[k] = bt * dl.a[k] + gm * nsv * Nst.a[k];
+#pragma unroll
+          for (int i = 0; i < D; ++i) dtau(i, i) += al * trs;
+#pragma unroll
+          for (int m = 0; m < D; ++m)
+#pragma unroll
+            for (int i = 0; i < D; ++i) {
+              double v = -P(i, n) * Fi(m, j);
+#pragma unroll
+              for (int r = 0; r < D; ++r) v += dtau(i, r) * Fi(m, r);
+              put_tangent(a, px, D2 * D2, (i + D * m) + D2 * (j + D * n), v);
+            }
+        }
+    } else {
     double ns[D];
 #pragma unroll
     for (int n = 0; n < D; ++n) {
@@ -422,15 +503,15 @@ __global__ void __launch_bounds__(kMatThreads) k_material(const MaterialArgs a, 
       if (a.Kp64) store(a.Kp64, c * N + px, Kp[c]);
       if (a.Kp32) store(a.Kp32, c * N + px, Kp[c]);
     }
-    if (a.Kfull) {
-      double *K = a.Kfull + px * (long long)(D2 * D2);
+    if (a.Kfull || a.Kt64 || a.Kt32) {
 #pragma unroll
       for (int n = 0; n < D; ++n)
 #pragma unroll
         for (int j = 0; j < D; ++j)
 #pragma unroll
-          for (int c = 0; c < D2; ++c) K[c + D2 * (j + D * n)] = Kp[c + D2 * n];
+          for (int c = 0; c < D2; ++c) put_tangent(a, px, D2 * D2, c + D2 * (j + D * n), Kp[c + D2 * n]);
     }
+    }  // reference tangent
   }
   bool bad = false;
 #pragma unroll

@@ -74,6 +74,8 @@ template <> struct V2<double> { using T = double2; };
 
 constexpr int kMaxStages = 12;  // 5 bits per stage in AxisPlanD::rcode
 constexpr int kMaxMaterials = 256;
+// MaterialHyperElastoPlastic1 mode (MatParams::logm_mode) with the consistent tangent
+constexpr int kHep1Consistent = 2;
 
 // ---------------------------------------------------------------- FFT plans
 // Device view of a 1-D FFT plan for one axis.  A length-n transform runs as a
@@ -122,6 +124,8 @@ enum TangentKind : int {
   TK_FISO = 5,    // TK_FINITE with S rebuilt from F per application (isotropic LE1/LE3/LE4)
   TK_GSMALL = 6,  // small strain, per-material stiffness C (MaterialLinearElasticGeneric): dP = C:de
   TK_GFINITE = 7, // finite strain, per-material C: dP = dF S + F (C:(F^T dF))
+  TK_FULL = 8,    // stored per-pixel tangent K(i,m,j,n) (D^4 planes): dP = K:dF (the consistent
+                  // elasto-plastic tangent, and the elastic pixels of a cell that has it)
 };
 
 // Device data the CG operator reads (precision R).
@@ -134,6 +138,7 @@ template <typename R> struct TangentData {
   const uint8_t *mat = nullptr;      // [npx] material index (TK_MIXED)
   const uint8_t *law_kind = nullptr; // [kMaxMaterials]: TK_FINITE or TK_KPRIME (TK_MIXED)
   const R *C = nullptr;     // [nmat][D^4] stiffness per material (TK_GSMALL / TK_GFINITE)
+  const R *Kt = nullptr;    // [D^4][npx] per-pixel tangent planes, entry (i + D m) + D^2 (j + D n) (TK_FULL)
 };
 
 // CG scalar state, resident on the device (all FP64).
@@ -265,13 +270,18 @@ void dot_device(const Ra *a, const Rb *b, long long n, double *partial, double *
 template <typename R>
 void newton_update(double *F, const R *x, long long n, double *partial, double *out,
                    cudaStream_t s);
+// line-search trial F = F0 + lam x, with x.x and F.F into out[0], out[1]
+template <typename R>
+void newton_trial(double *F, const double *F0, const R *x, double lam, long long n, double *partial, double *out,
+                  cudaStream_t s);
 template <typename Rd, typename Rs>
 void convert(Rd *dst, const Rs *src, long long n, double scale, cudaStream_t s);
 
 // ---------------------------------------------------------------- materials (materials.cu)
 struct MatParams {
   int law;
-  int logm_mode;            // HEP1: 0 projector sum (reference), 1 spectral
+  int logm_mode;            // HEP1: 0 projector sum (reference), 1 spectral, 2 spectral with the
+                            // consistent Kirchhoff->PK1 tangent (kHep1Consistent)
   double lam, mu, K, tau_y0, H;
 };
 
@@ -292,6 +302,8 @@ struct MaterialArgs {
   double *S64, *Kp64, *Fc64;
   float *S32, *Kp32, *Fc32;
   double *Kfull;            // optional full tangent, AoS [npx][D^4] (API)
+  double *Kt64;             // TK_FULL: tangent planes [D^4][npx] in the CG precision (one set)
+  float *Kt32;
   int *nonfinite;           // device flag set when a non-finite stress appears
   int has_hep;              // any MaterialHyperElastoPlastic1 pixel in the cell
 };

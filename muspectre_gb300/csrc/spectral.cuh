@@ -259,9 +259,17 @@ template <int D, int TK, typename R> struct TangentLocal {
   R F[kFinite ? D2 : 1], S[kFinite ? D2 : 1];
   R Kp[kKprime ? D2 * D : 1];
   const R *Cm = nullptr;
+  const R *Kt = nullptr;  // TK_FULL: this pixel's first tangent entry (planes npx apart)
+  long long kstride = 0;
 
   __device__ __forceinline__ void load(const TangentData<R> &td, long long px, long long npx) {
     kind = TK;
+    if constexpr (TK == TK_FULL) {
+      // the D^4 entries are read while they are applied (apply), not held in registers
+      Kt = td.Kt + px;
+      kstride = npx;
+      return;
+    }
     if constexpr (TK == TK_MIXED) kind = td.law_kind[td.mat[px]];
     if constexpr (kGeneric) Cm = td.C + (size_t)td.mat[px] * (D2 * D2);
     if constexpr (TK == TK_SMALL || (kFinite && !kGeneric)) {
@@ -336,6 +344,14 @@ template <int D, int TK, typename R> struct TangentLocal {
       tangent_generic_finite<D, R>(in, F, S, Cm, out);
     } else if constexpr (TK == TK_KPRIME) {
       tangent_kprime<D, R>(in, Kp, out);
+    } else if constexpr (TK == TK_FULL) {
+#pragma unroll
+      for (int c = 0; c < D2; ++c) {
+        R v = R(0);
+#pragma unroll
+        for (int q = 0; q < D2; ++q) v += Kt[(long long)(c + D2 * q) * kstride] * in[q];
+        out[c] = v;
+      }
     } else {
       if (kind == TK_FINITE) tangent_finite<D, R>(in, F, S, lam, mu, out);
       else tangent_kprime<D, R>(in, Kp, out);

@@ -153,6 +153,7 @@ void dispatch_fwd(int dim, int tk, const LastArgs<R> &a, const Cfg &c, cudaStrea
   MUSG_FWD_CASE(2, TK_SMALL) MUSG_FWD_CASE(2, TK_FINITE) MUSG_FWD_CASE(2, TK_KPRIME) MUSG_FWD_CASE(2, TK_MIXED)
   MUSG_FWD_CASE(3, TK_SMALL) MUSG_FWD_CASE(3, TK_FINITE) MUSG_FWD_CASE(3, TK_KPRIME) MUSG_FWD_CASE(3, TK_MIXED)
   MUSG_FWD_CASE(2, TK_GSMALL) MUSG_FWD_CASE(2, TK_GFINITE) MUSG_FWD_CASE(3, TK_GSMALL) MUSG_FWD_CASE(3, TK_GFINITE)
+  MUSG_FWD_CASE(2, TK_FULL) MUSG_FWD_CASE(3, TK_FULL)
   if (sizeof(R) == 4) {
     MUSG_FWD_CASE(2, TK_FISO) MUSG_FWD_CASE(3, TK_FISO)
   }
@@ -297,6 +298,7 @@ int last_cg_reg(Spectral &sp, int tkind, LastArgs<R> a, int G, bool inv, cudaStr
       MUSG_FR(2, TK_SMALL) MUSG_FR(2, TK_FINITE) MUSG_FR(2, TK_KPRIME) MUSG_FR(2, TK_MIXED) MUSG_FR(2, TK_FISO)
       MUSG_FR(3, TK_SMALL) MUSG_FR(3, TK_FINITE) MUSG_FR(3, TK_KPRIME) MUSG_FR(3, TK_MIXED) MUSG_FR(3, TK_FISO)
       MUSG_FR(2, TK_GSMALL) MUSG_FR(2, TK_GFINITE) MUSG_FR(3, TK_GSMALL) MUSG_FR(3, TK_GFINITE)
+      MUSG_FR(2, TK_FULL) MUSG_FR(3, TK_FULL)
 #undef MUSG_FR
       throw Error(MUSG_ERR_ARGUMENT, "unsupported tangent kind");
     }

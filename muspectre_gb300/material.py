@@ -143,12 +143,21 @@ class _HEP1(_Material):
     law = L.LAW_HEP1
 
     @classmethod
-    def make(cls, cell, name, Young, Poisson, tau_y0, H, logm='projector'):
+    def make(cls, cell, name, Young, Poisson, tau_y0, H, logm='projector', tangent='reference'):
         """MaterialHyperElastoPlastic1(name, E, ν, τ_y0, H)
         (material_hyper_elasto_plastic1.cc:41-65).  ``logm='projector'`` is the
         reference formula (non-finite on repeated eigenvalues); ``'spectral'`` uses
-        V log(Λ) Vᵀ, identical for distinct eigenvalues."""
-        mode = {'projector': 0, 'spectral': 1}[logm]
+        V log(Λ) Vᵀ, identical for distinct eigenvalues.
+
+        ``tangent='reference'`` converts the Kirchhoff tangent to PK1 as the reference
+        does (materials_toolbox.hh:374-410, independent of j); ``'consistent'`` (an
+        extension, off by default) stores the exact dP/dF of P = τ F⁻ᵀ through the
+        derivative of the spectral logm, so that Newton-CG converges on heterogeneous
+        elasto-plastic cells.  It implies ``logm='spectral'`` and writes
+        εp.cur = εp.old + Δγ (the reference adds Δγ to stale contents)."""
+        if tangent not in ('reference', 'consistent'):
+            raise ValueError("tangent must be 'reference' or 'consistent'")
+        mode = 2 if tangent == 'consistent' else {'projector': 0, 'spectral': 1}[logm]
         return cls(cell, name, [Young, Poisson, tau_y0, H, float(mode)])
 
     def add_pixel(self, pixel):

@@ -15,6 +15,7 @@ from __future__ import annotations
 
 import ctypes as C
 from dataclasses import dataclass
+from typing import Optional
 
 import numpy as np
 
@@ -24,7 +25,9 @@ from ._lib import ConvergenceError, SolverError  # noqa: F401
 
 @dataclass
 class OptimizeResult:
-    """src/solver/solver_common.hh:50-67 (grad and stress are (nb_dof, 1) arrays)."""
+    """src/solver/solver_common.hh:50-67 (grad and stress are (nb_dof, 1) arrays), plus
+    ``hom_stress``: the pixel mean of the stress after the load step (D×D, reduced on
+    the device; available with ``return_fields=False`` too)."""
     grad: np.ndarray
     stress: np.ndarray
     success: bool
@@ -32,6 +35,7 @@ class OptimizeResult:
     message: str
     nb_it: int
     nb_fev: int
+    hom_stress: Optional[np.ndarray] = None
 
 
 class SolverBase:
@@ -115,11 +119,20 @@ class SolverCG(SolverBase):
         return x
 
 
-def newton_cg(cell, load_steps, solver, newton_tol, equil_tol=None, verbose=0, *, return_fields=True, **kw):
+def newton_cg(cell, load_steps, solver, newton_tol, equil_tol=None, verbose=0, *, return_fields=True,
+              line_search=False, **kw):
     """newton_cg(cell, ΔF₀ | [ΔF...], solver, newton_tol, equil_tol, verbose=0)
     (bind_py_solvers.cc:75-106).  A single D×D load returns one OptimizeResult, a
     list returns a list.  ``return_fields=False`` skips the per-step copies of the
-    strain and stress fields to the host (the arrays are then empty)."""
+    strain and stress fields to the host (the arrays are then empty).
+
+    ``line_search=True`` (an extension, off by default) damps every Newton increment
+    by a backtracking line search on the norm of the projected residual: F = F0 + λ δF
+    with λ = 1, 1/2, ... until the norm falls below (1 - 1e-4 λ) of the current one
+    (or λ = 1/1024).  The convergence test still measures the full increment δF.  It
+    is what makes the consistent elasto-plastic tangent converge on heterogeneous
+    cells under large load increments."""
+    L.check(L.lib().musg_solver_set_line_search(solver.handle, 1 if line_search else 0))
     return _newton('musg_newton_cg', cell, load_steps, solver, newton_tol, equil_tol, verbose, return_fields, kw)
 
 
@@ -127,6 +140,7 @@ def de_geus(cell, load_steps, solver, newton_tol, equil_tol=None, verbose=0, *, 
     """de_geus(cell, ΔF₀ | [ΔF...], solver, newton_tol, equil_tol, verbose=0)
     (bind_py_solvers.cc:108-138, solvers.cc:220-408): each load step starts with the
     response to the macroscopic increment at the previous equilibrium."""
+    L.check(L.lib().musg_solver_set_line_search(solver.handle, 0))
     return _newton('musg_de_geus', cell, load_steps, solver, newton_tol, equil_tol, verbose, return_fields, kw)
 
 
@@ -155,5 +169,6 @@ def _newton(entry, cell, load_steps, solver, newton_tol, equil_tol, verbose, ret
         i = infos[k]
         out.append(OptimizeResult(grads[k].reshape(-1, 1) if return_fields else np.empty((0, 1)),
                                   stresses[k].reshape(-1, 1) if return_fields else np.empty((0, 1)),
-                                  bool(i.success), int(i.status), i.message.decode(), int(i.nb_it), int(i.nb_fev)))
+                                  bool(i.success), int(i.status), i.message.decode(), int(i.nb_it), int(i.nb_fev),
+                                  np.array(i.hom_stress[:d * d]).reshape(d, d).T))
     return out[0] if single else out

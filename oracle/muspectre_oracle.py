@@ -423,7 +423,7 @@ class MaterialHyperElastoPlastic1(Material):
 
     law = 'hep1'
 
-    def __init__(self, name, dim, young, poisson, tau_y0, H, logm_mode='projector'):
+    def __init__(self, name, dim, young, poisson, tau_y0, H, logm_mode='projector', tangent='reference'):
         super().__init__(name, dim)
         self.young, self.poisson = young, poisson
         self.lam = lame_lambda(young, poisson)
@@ -432,7 +432,11 @@ class MaterialHyperElastoPlastic1(Material):
         self.tau_y0, self.H = tau_y0, H
         # .cc:62: C = ½ C_T4(λ, μ) (Geers 2003 eq. 18)
         self.C = 0.5 * hooke_C(self.lam, self.mu, dim)
-        self.logm_mode = logm_mode
+        if tangent not in ('reference', 'consistent'):
+            raise ValueError(tangent)
+        # the consistent tangent (an extension, see evaluate_consistent) needs the spectral logm
+        self.tangent = tangent
+        self.logm_mode = 'spectral' if tangent == 'consistent' else logm_mode
         self._idx = 0
         self.F_prev = self.be_prev = self.eps_p = None
 
@@ -483,7 +487,13 @@ class MaterialHyperElastoPlastic1(Material):
             self._cur(self.F_prev)[:] = F
             ln_be = ln_be - 2 * dgamma[:, None, None] * N
             self._cur(self.be_prev)[:] = expm_sym(ln_be) if np.all(np.isfinite(ln_be)) else _expm_guard(ln_be)
-            self._cur(self.eps_p)[:] += dgamma
+            if self.tangent == 'consistent':
+                # the consistent mode writes εp.cur = εp.old + Δγ (every evaluation, so a
+                # repeated evaluation leaves the same state); the reference adds Δγ to the
+                # current buffer's stale contents (…plastic1.hh:262), kept in the other modes
+                self._cur(self.eps_p)[:] = self._old(self.eps_p) + dgamma
+            else:
+                self._cur(self.eps_p)[:] += dgamma
         is_plastic = phi > 0
         return tau, tau_eq, dgamma, N, is_plastic
 
@@ -506,8 +516,63 @@ class MaterialHyperElastoPlastic1(Material):
     def evaluate(self, F, form):
         if form != FINITE_STRAIN:
             raise RuntimeError("MaterialHyperElastoPlastic1 needs the finite-strain formulation")
+        if self.tangent == 'consistent':
+            return self.evaluate_consistent(F)
         tau, C = self.evaluate_stress_tangent_kirchhoff(F)
         return pk1_from_kirchhoff(F, tau, C)
+
+    def evaluate_consistent(self, F):
+        """Stress as in stress_n_internals (…plastic1.hh:228-271, spectral logm) and the
+        consistent tangent K(i,m,j,n) = dP(i,m)/dF(j,n) of P = τ F⁻ᵀ -- an extension: the
+        reference converts with the j-independent K' of materials_toolbox.hh:374-410.
+
+        With f = F F_prev⁻¹, be* = f be_old fᵀ = V diag(w) Vᵀ and the Kirchhoff tangent
+        C = α Itrac + β Isymm + γ N⊗N of …plastic1.hh:294-308 (the derivative of τ in
+        ln be*):
+          dbe*     = dF Mb + (dF Mb)ᵀ,  Mb = F_prev⁻¹ be_old fᵀ
+          d ln be* = V [g ∘ (Vᵀ dbe* V)] Vᵀ,  g(p,q) = (ln w_p - ln w_q)/(w_p - w_q), 1/w_p at p = q
+                     (the Daleckii-Krein formula for the derivative of the matrix logarithm)
+          dτ       = C : d ln be*
+          dP       = dτ F⁻ᵀ - P dFᵀ F⁻ᵀ
+        Column (j, n) of K is dP for dF = e_j e_nᵀ."""
+        d = self.dim
+        n = F.shape[0]
+        Fp = self._old(self.F_prev).copy()
+        be_old = self._old(self.be_prev).copy()
+        tau, tau_eq, dgamma, N, plastic = self.stress_n_internals(F)
+        Fpi = np.linalg.inv(Fp)
+        f = np.einsum('pij,pjk->pik', F, Fpi)
+        be_star = np.einsum('pij,pjk,plk->pil', f, be_old, f)
+        w, V = np.linalg.eigh(be_star)
+        Mb = np.einsum('pij,pjk,plk->pil', Fpi, be_old, f)
+        MV = np.einsum('pij,pjk->pik', Mb, V)
+        a_, b_ = w[:, :, None], w[:, None, :]
+        with np.errstate(divide='ignore', invalid='ignore'):
+            x = (a_ - b_) / b_
+            g = np.where(x == 0, 1.0 / b_, np.log1p(x) / (a_ - b_))
+        idx = np.arange(d)
+        g[:, idx, idx] = 1.0 / w
+        Nt = np.einsum('pbi,pbc,pcj->pij', V, N, V)
+        with np.errstate(divide='ignore', invalid='ignore'):
+            a0 = dgamma * self.mu / tau_eq
+        a1 = self.mu / (self.H + 3 * self.mu)
+        al = np.where(plastic, self.K / 2. - self.mu / 3 + a0 * self.mu, 0.5 * self.lam)
+        bt = np.where(plastic, (1 - 3 * a0) * self.mu, self.mu)
+        gm = np.where(plastic, 2 * self.mu * (a0 - a1), 0.0)
+        Fi = np.linalg.inv(F)
+        P = np.einsum('pij,pkj->pik', tau, Fi)
+        I = np.eye(d)
+        K = np.zeros((n, d, d, d, d))
+        for j in range(d):
+            for nn in range(d):
+                t = V[:, j, :, None] * MV[:, nn, None, :] + MV[:, nn, :, None] * V[:, j, None, :]
+                sm = g * t
+                trs = np.einsum('pii->p', sm)
+                nsv = np.einsum('pij,pij->p', Nt, sm)
+                dl = np.einsum('pik,pkl,pjl->pij', V, sm, V)
+                dtau = bt[:, None, None] * dl + (gm * nsv)[:, None, None] * N + (al * trs)[:, None, None] * I
+                K[:, :, :, j, nn] = np.einsum('pir,pmr->pim', dtau, Fi) - P[:, :, nn, None] * Fi[:, None, :, j]
+        return P, K
 
 
 def _expm_guard(ln_be):
@@ -843,9 +908,29 @@ def check_symmetry(eps, rel_tol=1e-8):
     return bool(rel_tol >= np.linalg.norm(eps - eps.T) / n if n > 0 else True) or rel_tol >= n
 
 
-def newton_cg(cell, load_steps, solver, newton_tol, equil_tol, verbose=0):
+def _line_search(cell, incrF, nr):
+    """Backtracking (Armijo) line search on the norm of the projected residual G(-P),
+    an extension of newton_cg (off by default): F = F0 + λ δF with λ = 1, 1/2, …, the
+    first λ whose residual norm is below (1 - 1e-4 λ) times the current one, or
+    λ = 1/1024.  Returns the projected residual at the accepted point and its norm
+    (the next Newton iteration starts from this evaluation)."""
+    F0 = cell.F.copy()
+    lam = 1.0
+    while True:
+        cell.F = F0 + lam * incrF
+        P, _ = cell.evaluate_stress_tangent()
+        rhs = cell.apply_projection(-P)
+        n2 = math.sqrt(float(rhs @ rhs))
+        if n2 < (1.0 - 1e-4 * lam) * nr or lam <= 1.0 / 1024:
+            return rhs, n2
+        lam *= 0.5
+
+
+def newton_cg(cell, load_steps, solver, newton_tol, equil_tol, verbose=0, line_search=False):
     """solvers.cc:44-217.  ``load_steps``: one D×D matrix or a list of them.
-    Returns a list of OptimizeResult for a list input, one result otherwise."""
+    Returns a list of OptimizeResult for a list input, one result otherwise.
+    ``line_search`` (an extension, off by default) damps each Newton increment by
+    :func:`_line_search`; the convergence test still measures the full increment δF."""
     single = isinstance(load_steps, np.ndarray) and load_steps.ndim == 2
     steps = [np.asarray(load_steps, dtype=float)] if single else [np.asarray(s, dtype=float) for s in load_steps]
     d = cell.dim
@@ -887,15 +972,22 @@ def newton_cg(cell, load_steps, solver, newton_tol, equil_tol, verbose=0):
             return state['conv']
 
         newt_iter = 0
+        evaluated = False
         while newt_iter < solver.get_maxiter() and not state['conv']:
-            P, _ = cell.evaluate_stress_tangent()
-            rhs = -P
-            rhs = cell.apply_projection(rhs)
-            stress_norm = math.sqrt(float(rhs @ rhs))
+            if not evaluated:
+                P, _ = cell.evaluate_stress_tangent()
+                rhs = -P
+                rhs = cell.apply_projection(rhs)
+                stress_norm = math.sqrt(float(rhs @ rhs))
+            evaluated = False
             if convergence_test():
                 break
             incrF = solver.solve(rhs)
-            cell.F = cell.F + incrF
+            if line_search:
+                rhs, stress_norm = _line_search(cell, incrF, stress_norm)
+                evaluated = True
+            else:
+                cell.F = cell.F + incrF
             incr_norm = math.sqrt(float(incrF @ incrF))
             grad_norm = math.sqrt(float(cell.F @ cell.F))
             if verbose > 0:

@@ -1,0 +1,105 @@
+"""MaterialHyperElastoPlastic1 with the consistent Kirchhoff->PK1 tangent (an opt-in
+extension; the reference's conversion, materials_toolbox.hh:374-410, is independent
+of j and its CG operator diverges on heterogeneous elasto-plastic cells) and newton_cg
+with the backtracking line search, on the GPU against the oracle's restatement:
+
+* per pixel: stress and full tangent over evaluations and history cycles (1e-11);
+* a heterogeneous two-phase Voronoi cell (the 64³ workload's materials and load path
+  on an odd 9³ grid) over four load steps in FP64: the same Newton step count per
+  load step, CG counts within 1%, strain field and homogenised stress to 1e-10;
+* the mixed-precision solve of the same cell: homogenised stress within 1e-6 of the
+  FP64 one at every step.
+"""
+import numpy as np
+import pytest
+
+from oracle import muspectre_oracle as o
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope='module')
+def mu():
+    import muspectre_gb300 as m
+    if m.device_count() < 1:
+        pytest.fail('no CUDA device visible')
+    return m
+
+
+def rel(a, b):
+    a = np.asarray(a, dtype=float)
+    b = np.asarray(b, dtype=float)
+    return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)
+
+
+def _voronoi_pair(mu, n=9, nseeds=8):
+    from muspectre_gb300 import workloads
+    w = workloads.voronoi(n=n, nseeds=nseeds, nsteps=20)
+    ocell = o.Cell(w['res'], w['lengths'], o.FINITE_STRAIN)
+    gcell = mu.Cell(w['res'], w['lengths'], mu.Formulation.finite_strain)
+    for ph, mask in (('A', w['phaseA']), ('B', ~w['phaseA'])):
+        p = w[ph]
+        m = ocell.add_material(o.MaterialHyperElastoPlastic1(ph, 3, p['E'], p['nu'], p['tau_y0'], p['H'],
+                                                             tangent='consistent'))
+        m.pixels = list(np.flatnonzero(mask))
+        mu.material.MaterialHyperElastoPlastic1_3d.make(gcell, ph, p['E'], p['nu'], p['tau_y0'], p['H'],
+                                                       tangent='consistent').add_pixels(mask)
+    return w, ocell, gcell
+
+
+def test_consistent_tangent_per_pixel(mu):
+    """Stress and dP/dF on a heterogeneous cell (two elasto-plastic phases and an
+    elastic one) at random states, over evaluations and a history cycle."""
+    rng = np.random.default_rng(3)
+    res = [5, 3, 3]
+    n = int(np.prod(res))
+    ocell = o.Cell(res, [1., 1., 1.], o.FINITE_STRAIN)
+    gcell = mu.Cell(res, [1., 1., 1.], mu.Formulation.finite_strain)
+    owner = rng.integers(0, 3, n)
+    for k, (E, nu, ty, H) in enumerate(((200e9, .3, 200e6, 1e9), (70e9, .33, 100e6, .5e9), (100e9, .25, None, None))):
+        idx = np.flatnonzero(owner == k)
+        if ty is None:
+            om = ocell.add_material(o.MaterialLinearElastic1('e', 3, E, nu))
+            mu.material.MaterialLinearElastic1_3d.make(gcell, 'e', E, nu).add_pixels(idx)
+        else:
+            om = ocell.add_material(o.MaterialHyperElastoPlastic1('p%d' % k, 3, E, nu, ty, H, tangent='consistent'))
+            mu.material.MaterialHyperElastoPlastic1_3d.make(gcell, 'p%d' % k, E, nu, ty, H,
+                                                           tangent='consistent').add_pixels(idx)
+        om.pixels = list(idx)
+    F = np.eye(3) + 0.004 * rng.standard_normal((n, 3, 3))
+    F[0] = np.diag([1.003, 1.0, 1.0])  # repeated eigenvalues of be*
+    for it in range(3):
+        ocell.F = o.t2_to_vec(F)
+        P, K = ocell.evaluate_stress_tangent()
+        gP, gK = gcell.evaluate_stress_tangent(o.t2_to_vec(F).reshape(n, -1).T, return_tangent=True)
+        assert rel(gP.T.reshape(-1), P) < 1e-11
+        assert rel(gK.T.reshape(-1), o.t4_to_vec(K)) < 1e-11
+        ocell.save_history_variables()
+        gcell.save_history_variables()
+        F = F + 0.003 * rng.standard_normal((n, 3, 3))
+
+
+def test_voronoi_steps_fp64_vs_oracle(mu):
+    w, ocell, gcell = _voronoi_pair(mu)
+    steps = w['steps'][:4]
+    ro = o.newton_cg(ocell, steps, o.SolverCG(ocell, 1e-8, 3000), 1e-6, 0.0, 0, line_search=True)
+    rg = mu.solvers.newton_cg(gcell, steps, mu.solvers.SolverCG(gcell, 1e-8, 3000), 1e-6, 0.0, line_search=True)
+    for a, b in zip(rg, ro):
+        assert a.success and b.success
+        assert a.nb_it == b.nb_it, ([x.nb_it for x in rg], [x.nb_it for x in ro])
+        assert abs(a.nb_fev - b.nb_fev) <= max(1, 0.01 * b.nb_fev), (a.nb_fev, b.nb_fev)
+        assert rel(a.grad, b.grad) < 1e-10
+        assert rel(o.homogenised(a.stress, 3), o.homogenised(b.stress, 3)) < 1e-10
+        assert rel(a.hom_stress, o.homogenised(b.stress, 3)) < 1e-10
+
+
+def test_voronoi_steps_mixed_vs_fp64(mu):
+    out = {}
+    for prec in ('fp64', 'mixed'):
+        w, _, gcell = _voronoi_pair(mu)
+        rs = mu.solvers.newton_cg(gcell, w['steps'][:4], mu.solvers.SolverCG(gcell, 1e-8, 3000, precision=prec),
+                                  1e-6, 0.0, line_search=True)
+        assert all(r.success for r in rs), prec
+        out[prec] = [o.homogenised(r.stress, 3) for r in rs]
+    for a, b in zip(out['mixed'], out['fp64']):
+        assert rel(a, b) < 1e-6, rel(a, b)
