@@ -162,7 +162,28 @@ def algorithmic_bytes(name, npx, nk, d2, s, tm):
         'axis1_inv': 2 * spec,
         'last_axis_inv_dot': spec + 2 * u,                 # spectrum in; p in; Ap out
         'cg_update': 6 * u,                                # x, p, r, Ap in; x, r out
+        'last_axis_fwd_tangent_alpha': 3 * u + tm * npx + spec,  # the same, and p.(K:p) -> alpha
+        'cg_update_x': 3 * u,                              # x, p in; x out
+        'last_axis_inv_update_r': spec + 2 * u,            # spectrum, r in; r out
     }.get(name, 0)
+
+
+def fp64_flops(name, npx, nk, res, d2=9):
+    """Floating-point operations of one launch of an FP64 CG-iteration kernel (finite-strain
+    LE1 tangent), counted as 5 m log2 m per complex transform of length m (two real rows
+    share one; 2 more per real entry to unpack), about 200 per pixel for dP = K:dF from F
+    and S, 100 per k-point for the Green operator of a row triple, 2 per vector entry
+    per axpy or dot."""
+    L, n1, n0 = res[2], res[1], res[0]
+    last = d2 * (2.5 * np.log2(L) + 2.0)
+    return {
+        'last_axis_fwd_tangent': npx * (last + 200 + 2 * d2),
+        'axis1_fwd': nk * d2 * 5 * np.log2(n1),
+        'green_axis0': nk * (d2 * 10 * np.log2(n0) + 100),
+        'axis1_inv': nk * d2 * 5 * np.log2(n1),
+        'last_axis_inv_dot': npx * (last + 2 * d2),
+        'cg_update': npx * d2 * 6,
+    }.get(name, 0.0)
 
 
 def measured_traffic(kernel, n):
@@ -221,15 +242,15 @@ def cpu_baseline(w, nit):
     return smp.describe(smp.cg_iteration_seconds(nit), REF_NEWTON_STEPS, REF_CG_ITERS, nit)
 
 
-def extra_configs(mu, workloads):
-    """The other workloads of the metric, each measured once on this GPU (N=1 only):
-    README case in FP64; 256^3 lognormal LE4 with six load cases batched; 64^3
-    two-phase HEP1 (the reference method's outcome); a Poisson request stream through
-    the continuous-batching server (solves/s, p50/p99 latency)."""
+def hom_err(a, b):
+    a = np.asarray(a, dtype=float)
+    b = np.asarray(b, dtype=float)
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+def readme_config(mu, workloads):
+    """README example (51x51 small strain), FP64: the reference's own CPU-runnable case."""
     import torch
-    from muspectre_gb300 import serving
-    out = {}
-    # README example, FP64 (the reference's own CPU-runnable case)
     w = workloads.readme_disc()
     times = []
     for _ in range(3):
@@ -242,57 +263,172 @@ def extra_configs(mu, workloads):
                                  w['newton_tol'], w['equil_tol'])
         hs = cell.homogenised_stress()
         times.append(time.perf_counter() - t0)
-    out['readme_51x51_fp64'] = {'ms_per_solve': 1e3 * statistics.median(times[1:]), 'newton_steps': r.nb_it,
-                                'cg_iters': r.nb_fev, 'success': bool(r.success),
-                                'hom_stress': [float(x) for x in hs.reshape(-1)],
-                                'includes': 'cell construction, upload, solve, homogenised stress'}
-    # 256^3 small-strain LE4, six unit load cases batched (one launch per pass for all)
-    w = workloads.lognormal(256)
+    return {'ms_per_solve': 1e3 * statistics.median(times[1:]), 'newton_steps': r.nb_it,
+            'cg_iters': r.nb_fev, 'success': bool(r.success),
+            'hom_stress': [float(x) for x in hs.reshape(-1)],
+            'includes': 'cell construction, upload, solve, homogenised stress'}
+
+
+def lognormal_config(mu, workloads, peak, n=256, repeats=3):
+    """n^3 small-strain LE4 (lognormal E), six unit load cases batched as right-hand
+    sides of one microstructure (one launch per CG pass for all six).  Mixed precision:
+    a first (untimed) solve captures the CUDA graphs, then the median of `repeats` warm
+    solves; FP64: one batched solve of the same cells; per load case the
+    homogenised-stress error of the mixed result against the FP64 one.  px.it/s counts
+    pixels x CG iterations x right-hand sides; its roofline fraction uses the CG
+    iteration's algorithmic bytes (16 field passes + the Lame planes per px.it, FP32),
+    so the Newton-level FP64 work makes it a lower bound."""
+    import torch
+    w = workloads.lognormal(n)
     cells = []
     for _ in w['loads']:
         c = mu.Cell(w['res'], w['lengths'], mu.Formulation.small_strain, allow_even=True)
         mu.material.MaterialLinearElastic4_3d.make(c, 'm').add_pixels(np.arange(c.nb_pixels), w['E'], w['nu'])
         c.initialise(mu.FFT_PlanFlags.measure)
         cells.append(c)
-    bs = mu.batch.BatchSolver(cells, w['cg_tol'], w['maxiter'], precision='mixed')
     loads = np.stack(w['loads'])[:, None]
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    res = bs.newton_cg(loads, w['newton_tol'], w['equil_tol'], return_stress=False)
-    torch.cuda.synchronize()
-    dt = time.perf_counter() - t0
-    cg = [r[0].nb_fev for r in res]
     npx = cells[0].nb_pixels
-    out['lognormal256_le4_6rhs_mixed'] = {
-        'seconds': dt, 'rhs_solves_per_s': len(cells) / dt, 'cg_iters_per_rhs': cg,
-        'pxit_per_s': npx * sum(cg) / dt, 'success': all(r[0].success for r in res),
-        'hom_stress_rhs0': [float(x) for x in cells[0].homogenised_stress().reshape(-1)],
-        'includes': 'first batched solve (CUDA-graph capture included), cells resident'}
-    del bs, cells
-    # 64^3 HEP1 on a two-phase Voronoi, F11 ramp in 20 steps
-    w = workloads.voronoi(64)
-    cell = mu.Cell(w['res'], w['lengths'], mu.Formulation.finite_strain, allow_even=True)
-    for ph, mask in (('A', w['phaseA']), ('B', ~w['phaseA'])):
-        p = w[ph]
-        mu.material.MaterialHyperElastoPlastic1_3d.make(cell, ph, p['E'], p['nu'], p['tau_y0'], p['H']).add_pixels(mask)
+    bs = mu.batch.BatchSolver(cells, w['cg_tol'], w['maxiter'], precision='mixed')
+    res = bs.newton_cg(loads, w['newton_tol'], w['equil_tol'], return_stress=False)  # graph capture, warm-up
+    c_prev = [r[0].nb_fev for r in res]
+    times, per_solve = [], []
+    for _ in range(repeats):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        res = bs.newton_cg(loads, w['newton_tol'], w['equil_tol'], return_stress=False)
+        torch.cuda.synchronize()
+        times.append(time.perf_counter() - t0)
+        per_solve = [r[0].nb_fev - p for r, p in zip(res, c_prev)]  # cumulative counters
+        c_prev = [r[0].nb_fev for r in res]
+    hm = [r[0].hom_stress for r in res]
+    del bs
+    b64 = mu.batch.BatchSolver(cells, w['cg_tol'], w['maxiter'], precision='fp64')
+    torch.cuda.synchronize()
     t0 = time.perf_counter()
+    r64 = b64.newton_cg(loads, w['newton_tol'], w['equil_tol'], return_stress=False)
+    torch.cuda.synchronize()
+    t64 = time.perf_counter() - t0
+    errs = [hom_err(a, b[0].hom_stress) for a, b in zip(hm, r64)]
+    dt = statistics.median(times)
+    pxit = npx * sum(per_solve) / dt
+    bpx = 16 * 9 * 4 + 8  # FP32 fields per px.it of the fused CG iteration + lambda, mu
+    return {'seconds_median': dt, 'seconds_all': times, 'rhs_solves_per_s': len(cells) / dt,
+            'cg_iters_per_rhs': per_solve, 'newton_steps': [r[0].nb_it for r in res],
+            'pxit_per_s': pxit, 'cg_bytes_per_pxit': bpx,
+            'roofline_frac_lower_bound': pxit * bpx / (peak * 1e9),
+            'success': all(r[0].success for r in res), 'fp64_seconds': t64,
+            'fp64_cg_iters_per_rhs': [r[0].nb_fev for r in r64],
+            'stress_rel_err_vs_fp64_per_rhs': errs, 'stress_rel_err_vs_fp64_max': max(errs),
+            'includes': 'warm batched solves (graphs captured by an untimed first solve), cells resident'}
+
+
+def voronoi_config(mu, workloads, n=64):
+    """n^3 two-phase HyperElastoPlastic1 on a periodic Voronoi of 32 grains, F11 ramped to
+    1.05 in 20 load steps with the state on the device.  The reference method
+    (projector logm, j-independent Kirchhoff tangent) ends in ConvergenceError at the
+    first step; solved here with the consistent tangent and newton_cg's line search
+    (both opt-in extensions): FP64 return mapping, FP32 inner CG (mixed), against the
+    same solve in FP64 (the homogenised-stress error at every step)."""
+    import torch
+    w = workloads.voronoi(n)
+
+    def cell_for(tangent):
+        c = mu.Cell(w['res'], w['lengths'], mu.Formulation.finite_strain, allow_even=True)
+        for ph, mask in (('A', w['phaseA']), ('B', ~w['phaseA'])):
+            p = w[ph]
+            mu.material.MaterialHyperElastoPlastic1_3d.make(c, ph, p['E'], p['nu'], p['tau_y0'], p['H'],
+                                                           tangent=tangent).add_pixels(mask)
+        c.initialise(mu.FFT_PlanFlags.measure)
+        return c
+
+    out = {}
+    c = cell_for('reference')
     try:
-        rs = mu.solvers.newton_cg(cell, w['steps'], mu.solvers.SolverCG(cell, w['cg_tol'], 400, precision='mixed'),
-                                  w['newton_tol'], w['equil_tol'], return_fields=False)
-        status = 'solved %d steps' % len(rs)
+        mu.solvers.newton_cg(c, w['steps'], mu.solvers.SolverCG(c, w['cg_tol'], 400, precision='mixed'),
+                             w['newton_tol'], w['equil_tol'], return_fields=False)
+        out['reference_method_status'] = 'solved'
     except mu.ConvergenceError as e:
-        status = 'ConvergenceError: ' + str(e)[:90]
-    out['voronoi64_hep1_20steps'] = {
-        'status': status, 'seconds': time.perf_counter() - t0,
-        'note': 'the reference method (projector logm, j-independent Kirchhoff tangent) does not solve this '
-                'configuration; the oracle and the FP64 GPU path end the same way'}
-    # request stream through the server
-    reqs = [serving.c5_request(i, 1000 + i) for i in range(48)]
-    srv = serving.Server(96 << 30, lanes=4, max_batch=8, precision='mixed')
-    st = serving.run_stream(reqs, rate_hz=100.0, server=srv)
-    st.update({'arrivals': 'Poisson 100/s', 'lanes': 4, 'hbm_budget_bytes': 96 << 30})
-    out['serving_stream_mixed'] = st
+        out['reference_method_status'] = 'ConvergenceError: ' + str(e)[:80]
+    del c
+    res = {}
+    for prec in ('mixed', 'fp64'):
+        c = cell_for('consistent')
+        s = mu.solvers.SolverCG(c, w['cg_tol'], w['maxiter'], precision=prec)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        rs = mu.solvers.newton_cg(c, w['steps'], s, w['newton_tol'], w['equil_tol'], return_fields=False,
+                                  line_search=True)
+        torch.cuda.synchronize()
+        res[prec] = (time.perf_counter() - t0, rs)
+        del c, s
+    tm, rm = res['mixed']
+    t64, r64 = res['fp64']
+    errs = [hom_err(a.hom_stress, b.hom_stress) for a, b in zip(rm, r64)]
+    out.update({'solves_per_s': 1.0 / tm, 'seconds': tm, 'load_steps': len(rm),
+                'success': all(r.success for r in rm),
+                'newton_steps_per_load_step': [r.nb_it for r in rm], 'cg_iters_total': rm[-1].nb_fev,
+                'fp64_seconds': t64, 'fp64_newton_steps_per_load_step': [r.nb_it for r in r64],
+                'fp64_cg_iters_total': r64[-1].nb_fev, 'speedup_vs_fp64': t64 / tm,
+                'stress_rel_err_vs_fp64_max': max(errs), 'stress_rel_err_vs_fp64_last': errs[-1],
+                'hom_stress_11_mpa': [float(r.hom_stress[0, 0]) / 1e6 for r in rm],
+                'method': 'consistent Kirchhoff->PK1 tangent, spectral logm, Armijo line search (extensions)'})
     return out
+
+
+def serving_config(mu, nreq=2000, lanes=4, max_batch=8, budget=96 << 30, sweep_n=200, sample=20):
+    """The serving stream: nreq seeded requests of mixed size, formulation, law and
+    load path through the continuous-batching server (mixed precision).  Capacity: all
+    nreq submitted at once (open loop, far past saturation).  Rate sweep: sweep_n
+    requests at Poisson rates of 1/4, 1/2, 1 and 2 times that capacity, each on a
+    fresh server (succeeded solves/s, p50/p99 latency).  Accuracy: a seeded sample of
+    `sample` requests solved again alone in FP64 (the plain method, whose parity with
+    the oracle the tests pin); the homogenised-stress error of the served mixed result
+    against it."""
+    from muspectre_gb300 import serving
+    t0 = time.perf_counter()
+    reqs = [serving.c5_request(i, 1000 + i) for i in range(nreq)]
+    t_gen = time.perf_counter() - t0
+    srv = serving.Server(budget, lanes=lanes, max_batch=max_batch, precision='mixed')
+    cap = serving.run_stream(reqs, rate_hz=0, server=srv)
+    mixed = dict(srv.results)
+    del srv
+    capacity = cap['succeeded_per_s']
+    sweep = []
+    for f in (0.25, 0.5, 1.0, 2.0):
+        s2 = serving.Server(budget, lanes=lanes, max_batch=max_batch, precision='mixed')
+        st = serving.run_stream(reqs[:sweep_n], rate_hz=f * capacity, server=s2, seed=77)
+        sweep.append({'offered_hz': f * capacity, 'succeeded_per_s': st['succeeded_per_s'],
+                      'p50_ms': st['p50_ms_succeeded'], 'p99_ms': st['p99_ms_succeeded'],
+                      'succeeded': st['succeeded'], 'requests': st['requests'], 'batches': st['batches']})
+        del s2
+    rng = np.random.default_rng(7)
+    picked = sorted(int(i) for i in rng.choice(nreq, size=sample, replace=False))
+    errs = {}
+    for i in picked:
+        m = mixed.get(i)
+        if m is None or not m.success:
+            continue
+        r64 = serving.solve_alone(reqs[i], precision='fp64')
+        if r64.success:
+            errs[i] = hom_err(m.stress, r64.stress)
+    laws = [sorted({m[0] for m in r.materials}) for r in reqs]
+    cap.update({'arrivals': 'all %d submitted at once (open loop)' % nreq, 'lanes': lanes, 'max_batch': max_batch,
+                'hbm_budget_bytes': budget, 'request_generation_s': t_gen,
+                'elasto_plastic_requests': sum('hep1' in l for l in laws),
+                'rate_sweep': sweep,
+                'fp64_sample': {'requests': picked, 'compared': len(errs),
+                                'stress_rel_err_max': max(errs.values()) if errs else None,
+                                'stress_rel_err_median': float(np.median(list(errs.values()))) if errs else None,
+                                'within_1e-6': sum(e <= 1e-6 for e in errs.values())}})
+    return cap
+
+
+def extra_configs(mu, workloads, peak):
+    """The other workloads of the metric, each measured on this GPU (N=1 only)."""
+    return {'readme_51x51_fp64': readme_config(mu, workloads),
+            'lognormal256_le4_6rhs_mixed': lognormal_config(mu, workloads, peak),
+            'voronoi64_hep1_20steps': voronoi_config(mu, workloads),
+            'serving_stream_mixed': serving_config(mu)}
 
 
 def run_reference(args, rank, world):
@@ -462,6 +598,15 @@ def main():
     fp64_sps = 1.0 / statistics.median(fp64_lat)
     fp64_cg = r64.nb_fev  # cumulative counter: divide by solves done with this solver
     fp64_cg_per_solve = fp64_cg / (1 + args.fp64_steps)
+    # the FP64 kernels against the measured FP64 FMA throughput (their bound)
+    fp64_peak = mu._lib.probe_fp64_fma()
+    prof64 = fp64.profile(5)
+    k64 = {}
+    for name, ms in prof64.items():
+        fl = fp64_flops(name, npx, nk, w['res'])
+        k64[name] = {'ms': ms, 'tflops': fl / (ms * 1e-3) / 1e12 if ms > 0 else None,
+                     'frac_of_fp64_fma': (fl / (ms * 1e-3) / 1e12) / fp64_peak if ms > 0 else None,
+                     'gbs': algorithmic_bytes(name, npx, nk, d2, 8, 8 * 18) / (ms * 1e-3) / 1e9 if ms > 0 else None}
 
     # ---------------- end to end through the public API from host buffers
     e2e_t = []
@@ -491,7 +636,9 @@ def main():
         'latency_ms': {'p50': float(np.percentile(lat_ms, 50)), 'p99': float(np.percentile(lat_ms, 99))},
         'newton_steps': newton_mixed, 'cg_iters_per_solve': cg_per_solve,
         'pxit_per_s': value * npx * cg_per_solve / world * world,
-        'fp64': {'solves_per_s': fp64_sps, 'cg_iters_per_solve': fp64_cg_per_solve, 'newton_steps': r64.nb_it},
+        'fp64': {'solves_per_s': fp64_sps, 'cg_iters_per_solve': fp64_cg_per_solve, 'newton_steps': r64.nb_it,
+                 'fp64_fma_peak_tflops': fp64_peak, 'peak_source': 'measured (probe kernel of FMA chains)',
+                 'kernels': k64},
         'speedup_vs_fp64': value / world / fp64_sps,
         'stress_rel_err_vs_fp64': err,
         'roofline': roof,
@@ -501,7 +648,7 @@ def main():
         'e2e': {'value': e2e_v, 'unit': 'solves/s', 'h2d_bytes_per_step': h2d, 'd2h_bytes_per_step': d2h},
     }
     if rank == 0 and world == 1 and not args.no_extra:
-        line['configs'] = extra_configs(mu, workloads)
+        line['configs'] = extra_configs(mu, workloads, peak)
     if rank == 0 and not args.no_cpu:
         cb = cpu_baseline(w, args.cpu_cg_iters)
         line['cpu_baseline'] = {'value': cb['solves_per_s'], 'unit': 'solves/s', 'cores': cb['cores'], 'kind': 'port',

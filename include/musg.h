@@ -299,9 +299,11 @@ int musg_server_wait(musg_server *srv, long long id, double timeout_s, musg_serv
 int musg_server_get_stats(musg_server *srv, musg_server_stats *out);
 /* closes the server and joins its lanes */
 int musg_server_destroy(musg_server *srv);
-/* the admission step of a lane: the oldest waiting request that fits the budget
- * (or any request when nothing runs) and the waiting requests of its shape that fit
- * too, at most cap; their ids, count and bytes (now counted as in use) */
+/* the admission step of a lane: the oldest waiting request that fits the budget next
+ * to the running ones and the waiting requests of its shape that fit too, at most cap
+ * (a request with the consistent elasto-plastic tangent, solved with the line search,
+ * is taken alone); their ids, count and bytes (now counted as in use).  A request
+ * larger than the whole budget is refused by musg_server_submit (MUSG_ERR_MEMORY). */
 int musg_server_admit(musg_server *srv, long long *ids, int cap, int *count, unsigned long long *bytes);
 /* returns bytes of a finished group to the budget */
 int musg_server_release(musg_server *srv, unsigned long long bytes);
@@ -315,6 +317,10 @@ int musg_server_release(musg_server *srv, unsigned long long bytes);
  *   cell's last projected residual; ms_out needs 8 entries; kernel names by
  *   musg_solver_kernel_name.  Needs an evaluated tangent (after newton_cg). */
 int musg_launch_count(unsigned long long *count);
+/* measured FP64 FMA throughput of the current device in TFLOP/s (a probe kernel of
+ * independent fused multiply-add chains on every SM, best of three timed launches):
+ * the bound of the FP64 passes, whose arithmetic intensity is about 1 flop/byte */
+int musg_probe_fp64_fma(double *tflops);
 int musg_solver_profile(musg_solver *solver, int iterations, double *ms_out, int *nb_kernels);
 const char *musg_solver_kernel_name(musg_solver *solver, int k);
 

@@ -101,6 +101,7 @@ _SIGNATURES = {
     'musg_solver_destroy': (C.c_int, [_P]),
     'musg_solver_set_inner_tol': (C.c_int, [_P, C.c_double]),
     'musg_solver_set_line_search': (C.c_int, [_P, C.c_int]),
+    'musg_probe_fp64_fma': (C.c_int, [C.POINTER(C.c_double)]),
     'musg_solver_get_counter': (C.c_int, [_P, C.POINTER(C.c_uint)]),
     'musg_solver_reset_counter': (C.c_int, [_P]),
     'musg_solver_has_converged': (C.c_int, [_P, _I]),
@@ -193,6 +194,13 @@ def launch_count():
     n = C.c_ulonglong(0)
     check(lib().musg_launch_count(C.byref(n)))
     return n.value
+
+
+def probe_fp64_fma():
+    """Measured FP64 FMA throughput of the current device (TFLOP/s)."""
+    t = C.c_double(0.0)
+    check(lib().musg_probe_fp64_fma(C.byref(t)))
+    return t.value
 
 
 def selftest_wait_timeout(limit_ms=5.0):

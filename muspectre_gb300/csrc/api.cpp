@@ -219,7 +219,9 @@ struct musg_cell {
     rhs.alloc(field_bytes());
     MUSG_CUDA(cudaMemsetAsync(F.p, 0, field_bytes(), stream));
     MUSG_CUDA(cudaMemsetAsync(P.p, 0, field_bytes(), stream));
-    partial.alloc((size_t)std::max<long long>(4 * 4096, 2 * sp.g.nrows + 64) * sizeof(double));
+    // reduction scratch: block or per-warp partial sums of the passes (at most 16 warps
+    // per half row pair of the last-axis passes)
+    partial.alloc((size_t)std::max<long long>(4 * 4096, 16 * sp.g.nrows + 64) * sizeof(double));
     scal.alloc(64 * sizeof(double));
     nonfinite.alloc(sizeof(int));
     MUSG_CUDA(cudaMemsetAsync(nonfinite.p, 0, sizeof(int), stream));
@@ -568,7 +570,8 @@ struct musg_solver {
     x.alloc(n * rbytes());
     r.alloc(n * rbytes());
     p.alloc(n * rbytes());
-    Ap.alloc(n * rbytes());
+    // the FP32 inner solve never stores Ap (its last pass updates r directly)
+    if (precision != MUSG_PRECISION_MIXED) Ap.alloc(n * rbytes());
     st.alloc(sizeof(CGState));
     MUSG_CUDA(cudaMemset(st.p, 0, sizeof(CGState)));
     MUSG_CUDA(cudaMallocHost(&hst, sizeof(CGState)));
@@ -579,27 +582,40 @@ struct musg_solver {
   }
 
   // one CG iteration (solver_cg.cc:76-97); ev, when given, receives an event
-  // before the first and after every kernel (profiling)
+  // before the first and after every kernel (profiling).  FP64: the operator passes
+  // (alpha by the last one) and cg_update (x, r, beta); FP32: the operator passes and
+  // cg_update_x, which carry the whole iteration (alpha from p.(K:p) in the first pass;
+  // r and beta in the last).
   template <typename R> int iteration(cudaStream_t s, cudaEvent_t *ev = nullptr) {
     musg_cell &c = *cell;
     const long long n = c.nb_dof();
     CGState *d = st.as<CGState>();
     double *part = c.partial.as<double>();
     const TangentData<R> td = c.tangent<R>();
-    const int nop = cg_operator<R>(c.sp, c.tk<R>(), td, d, r.as<R>(), p.as<R>(), Ap.as<R>(), part, s, ev);
-    (void)nop;  // the last pass finishes alpha over its own partial sums
-    int k = c.dim == 3 ? 5 : 3;
+    R *ap = sizeof(R) == 8 ? Ap.as<R>() : nullptr;
+    const int nop = cg_operator<R>(c.sp, c.tk<R>(), td, d, r.as<R>(), x.as<R>(), p.as<R>(), ap, part, s, ev);
+    (void)nop;
+    const int k = nb_kernels();
+    if (sizeof(R) == 4) return k;
     cg_update<R>(d, x.as<R>(), r.as<R>(), p.as<R>(), Ap.as<R>(), n, part, s);  // and beta
-    if (ev) MUSG_CUDA(cudaEventRecord(ev[++k], s));
+    if (ev) MUSG_CUDA(cudaEventRecord(ev[k], s));
     return k;  // number of kernels
   }
 
-  static const char *kernel_name(int dim, int k) {
+  // kernels per CG iteration: five (3-D) or three (2-D) passes and one vector kernel
+  int nb_kernels() const { return cell->dim == 3 ? 6 : 4; }
+
+  static const char *kernel_name(int dim, int precision, int k) {
     static const char *n3[] = {"last_axis_fwd_tangent", "axis1_fwd", "green_axis0", "axis1_inv", "last_axis_inv_dot",
                                "cg_update"};
     static const char *n2[] = {"last_axis_fwd_tangent", "green_axis0", "last_axis_inv_dot", "cg_update"};
-    if (dim == 3) return (k >= 0 && k < 6) ? n3[k] : "";
-    return (k >= 0 && k < 4) ? n2[k] : "";
+    static const char *f3[] = {"last_axis_fwd_tangent_alpha", "cg_update_x", "axis1_fwd", "green_axis0",
+                               "axis1_inv", "last_axis_inv_update_r"};
+    static const char *f2[] = {"last_axis_fwd_tangent_alpha", "cg_update_x", "green_axis0",
+                               "last_axis_inv_update_r"};
+    const char *const *t = precision == MUSG_PRECISION_MIXED ? (dim == 3 ? f3 : f2) : (dim == 3 ? n3 : n2);
+    const int nk = dim == 3 ? 6 : 4;
+    return (k >= 0 && k < nk) ? t[k] : "";
   }
 
   // mean per-kernel durations (ms) over `iters` eagerly launched iterations started
@@ -611,7 +627,7 @@ struct musg_solver {
     const long long n = c.nb_dof();
     double *part = c.partial.as<double>();
     cg_init<R>(st.as<CGState>(), c.rhs.as<double>(), r.as<R>(), x.as<R>(), n, 0.0, iters, part, part + 4096, s);
-    const int nk = c.dim == 3 ? 6 : 4;
+    const int nk = nb_kernels();
     std::vector<cudaEvent_t> ev(nk + 1);
     for (auto &e : ev) MUSG_CUDA(cudaEventCreate(&e));
     std::vector<double> acc(nk, 0.0);
@@ -749,8 +765,9 @@ struct musg_batch {
       tp[b].spec = sizeof(R) == 8 ? c.sp.spec64 : c.sp.spec32;
       tp[b].st = state(b);
       tp[b].r = sv.r.p;
+      tp[b].x = sv.x.p;
       tp[b].p = sv.p.p;
-      tp[b].Ap = sv.Ap.p;
+      tp[b].Ap = sizeof(R) == 8 ? sv.Ap.p : nullptr;  // the FP32 passes do not store Ap
       tp[b].partial = c.partial.as<double>();
       static_assert(sizeof(TangentData<R>) == sizeof(tp[b].td), "tangent table layout");
       memcpy(tp[b].td, &td, sizeof(td));
@@ -770,8 +787,9 @@ struct musg_batch {
   template <typename R> void iteration(cudaStream_t s) {
     musg_cell &c0 = *cells[0];
     const long long n = c0.nb_dof();
-    cg_operator_batch<R>(c0.sp, c0.tk<R>(), (const ProblemPtrs<R> *)tab_p.p, B(), s);  // and alpha
-    cg_update_batch<R>(tab_v.as<BatchVec<R>>(), n, B(), s);                              // and beta
+    cg_operator_batch<R>(c0.sp, c0.tk<R>(), (const ProblemPtrs<R> *)tab_p.p, tab_v.as<BatchVec<R>>(), B(),
+                         s);  // and alpha (FP32: the whole iteration)
+    if (sizeof(R) == 8) cg_update_batch<R>(tab_v.as<BatchVec<R>>(), n, B(), s);  // and beta
   }
 
   template <typename R> void build_graph() {
@@ -1142,10 +1160,12 @@ template <typename R> void cg_operator_once(musg_cell &c, const double *dF, doub
   const long long n = c.nb_dof();
   if (c.io2.bytes < c.field_bytes()) c.io2.alloc(c.field_bytes());
   c.upload_field(dF, c.io2.as<double>());
-  DevBuf r, p, Ap, st;
+  DevBuf r, x, p, Ap, st;
   r.alloc((size_t)n * sizeof(R));
+  x.alloc((size_t)n * sizeof(R));
   p.alloc((size_t)n * sizeof(R));
   Ap.alloc((size_t)n * sizeof(R));
+  MUSG_CUDA(cudaMemsetAsync(x.p, 0, (size_t)n * sizeof(R), c.stream));
   st.alloc(sizeof(CGState));
   // first CG iteration: p = -r, so r = -dF gives p = dF and Ap = G(K:dF)
   convert<R, double>(r.as<R>(), c.io2.as<double>(), n, -1.0, c.stream);
@@ -1153,7 +1173,8 @@ template <typename R> void cg_operator_once(musg_cell &c, const double *dF, doub
   h.maxiter = 1;
   h.active = 1;
   MUSG_CUDA(cudaMemcpyAsync(st.p, &h, sizeof(h), cudaMemcpyHostToDevice, c.stream));
-  cg_operator<R>(c.sp, c.tk<R>(), c.tangent<R>(), st.as<CGState>(), r.as<R>(), p.as<R>(), Ap.as<R>(),
+  // the kernels of the solver's iteration; the FP32 ones store Ap because it is given
+  cg_operator<R>(c.sp, c.tk<R>(), c.tangent<R>(), st.as<CGState>(), r.as<R>(), x.as<R>(), p.as<R>(), Ap.as<R>(),
                  c.partial.as<double>(), c.stream);
   convert<double, R>(c.io2.as<double>(), Ap.as<R>(), n, 1.0, c.stream);
   c.download_field(c.io2.as<double>(), dP);
@@ -1666,6 +1687,13 @@ int musg_solver_solve(musg_solver *solver, const double *rhs, double *x_out) {
   });
 }
 
+int musg_probe_fp64_fma(double *tflops) {
+  return guard([&] {
+    require(tflops, MUSG_ERR_ARGUMENT, "null argument");
+    *tflops = fp64_fma_tflops(nullptr);
+  });
+}
+
 int musg_launch_count(unsigned long long *count) {
   return guard([&] {
     require(count, MUSG_ERR_ARGUMENT, "null argument");
@@ -1684,7 +1712,7 @@ int musg_solver_profile(musg_solver *solver, int iterations, double *ms_out, int
 
 const char *musg_solver_kernel_name(musg_solver *solver, int k) {
   if (!solver || !solver->cell) return "";
-  return musg_solver::kernel_name(solver->cell->dim, k);
+  return musg_solver::kernel_name(solver->cell->dim, solver->precision, k);
 }
 
 int musg_batch_create(musg_cell **cells, int nb_cells, double tol, unsigned maxiter, int precision,

@@ -156,6 +156,80 @@ void cg_update(CGState *st, R *x, R *r, const R *p, const R *Ap, long long n, do
   MUSG_CHECK_LAUNCH();
 }
 
+// The part of a CG iteration of the FP32 inner solve that its spectral passes leave
+// out: cg_alpha sets alpha = r.r / p.(K:p) from the forward pass's nparts partial sums
+// (one block per problem, a fixed order), and cg_update_x applies x += alpha p.  Both
+// run between the forward pass (which writes p and the sums) and the inverse pass
+// (which may end the loop), so they are gated by the loop flag like them.
+template <typename R> __device__ __forceinline__ void update_x_body(R alpha, R *x, const R *p, long long n) {
+  using V = typename Vec16<R>::T;
+  constexpr int W = Vec16<R>::W;
+  const long long nv = n / W;
+  V *xv = reinterpret_cast<V *>(x);
+  const V *pv = reinterpret_cast<const V *>(p);
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < nv; i += (long long)gridDim.x * blockDim.x) {
+    V xi = xv[i];
+    const V pi = pv[i];
+    R *xs = reinterpret_cast<R *>(&xi);
+    const R *ps = reinterpret_cast<const R *>(&pi);
+#pragma unroll
+    for (int u = 0; u < W; ++u) xs[u] += alpha * ps[u];
+    xv[i] = xi;
+  }
+  if (blockIdx.x == 0)
+    for (long long i = nv * W + threadIdx.x; i < n; i += blockDim.x) x[i] += alpha * p[i];
+}
+
+// alpha = r.r / p.(K:p) of problem blockIdx.x (a table of states and partial arrays,
+// or one state and array)
+__global__ void k_cg_alpha(CGState *st, const double *partial, const BatchVec<float> *tab, int nparts) {
+  dep_wait();
+  CGState *s = tab ? tab[blockIdx.x].st : st;
+  const double *part = tab ? tab[blockIdx.x].partial : partial;
+  if (!s->active) return;
+  const double pAp = sum_partials_fresh(part, nparts);
+  if (threadIdx.x == 0) {
+    s->pAp = pAp;
+    s->alpha = s->rdr / pAp;
+  }
+}
+
+template <typename R> __global__ void k_cg_update_x(const CGState *st, R *x, const R *p, long long n) {
+  dep_wait();
+  if (!st->active) return;
+  update_x_body<R>(R(st->alpha), x, p, n);
+}
+
+template <typename R>
+void cg_update_x(const CGState *st, R *x, const R *p, long long n, const double *partial, int nparts,
+                 cudaStream_t s) {
+  if (!(aligned16(x) && aligned16(p))) throw Error(MUSG_ERR_ARGUMENT, "CG vectors must be 16-byte aligned");
+  launch_pdl(k_cg_alpha, dim3(1), dim3(1024), 0, s, const_cast<CGState *>(st), partial,
+             (const BatchVec<float> *)nullptr, nparts);
+  MUSG_CHECK_LAUNCH();
+  launch_pdl(k_cg_update_x<R>, dim3(update_blocks(n)), dim3(kRedThreads), 0, s, st, x, p, n);
+  MUSG_CHECK_LAUNCH();
+}
+
+template <typename R> __global__ void k_cg_update_x_b(const BatchVec<R> *tab, long long n) {
+  dep_wait();
+  const BatchVec<R> q = tab[blockIdx.y];
+  if (!q.st->active) return;
+  update_x_body<R>(R(q.st->alpha), q.x, q.p, n);
+}
+
+template <typename R> void cg_update_x_batch(const BatchVec<R> *tab, long long n, int nparts, int B, cudaStream_t s) {
+  launch_pdl(k_cg_alpha, dim3(B), dim3(1024), 0, s, (CGState *)nullptr, (const double *)nullptr,
+             (const BatchVec<float> *)tab, nparts);
+  MUSG_CHECK_LAUNCH();
+  launch_pdl(k_cg_update_x_b<R>, dim3(update_blocks(n), B), dim3(kRedThreads), 0, s, tab, n);
+  MUSG_CHECK_LAUNCH();
+}
+
+template void cg_update_x<float>(const CGState *, float *, const float *, long long, const double *, int,
+                                 cudaStream_t);
+template void cg_update_x_batch<float>(const BatchVec<float> *, long long, int, int, cudaStream_t);
+
 // ------------------------------------------------------------------ batched
 template <typename R>
 __global__ void k_cg_update_b(const BatchVec<R> *tab, long long n) {

@@ -206,14 +206,19 @@ void spectral_inverse(Spectral &sp, R *out, R scale, cudaStream_t s);
 template <typename R>
 void spectral_project(Spectral &sp, const R *in, R *out, R in_scale, cudaStream_t s);
 
-// CG operator application, fused: p = -r + beta p (or p = -r on the first
-// iteration), Ap = G(K:p), partial[b] = block sums of p.Ap, and alpha = r.r / p.Ap
-// in the state (by the last block of the last pass).  Returns the number of partial
-// sums written (blocks of the last pass).
-// ev (optional): an event is recorded before the first and after every kernel
+// CG operator application with the iteration's vector work fused into its passes.
+// FP64 (the reference's order): p = -r + beta p (or p = -r on the first iteration),
+// Ap = G(K:p), and alpha = r.r / p.Ap in the state (last block of the last pass);
+// cg_update completes the iteration.  FP32 (the mixed path's inner solve): the whole
+// iteration: the first pass writes the block sums of p.(K:p), cg_update_x sets
+// alpha = r.r / p.(K:p) and applies x += alpha p, the last pass r += alpha Ap, beta
+// and the loop condition; x is not
+// read in FP64, and Ap is written in FP32 only when non-null.  Returns the number of
+// partial sums written by the last pass.  ev (optional): an event is recorded before
+// the first and after every kernel
 template <typename R>
 int cg_operator(Spectral &sp, int tkind, const TangentData<R> &td, const CGState *st,
-                const R *r, R *p, R *Ap, double *partial, cudaStream_t s,
+                R *r, R *x, R *p, R *Ap, double *partial, cudaStream_t s,
                 cudaEvent_t *ev = nullptr);
 // plain operator (no CG state): out = G(K:in)
 template <typename R>
@@ -226,14 +231,17 @@ template <typename R> struct ProblemPtrs;
 struct ProblemPtrsHost {
   void *spec;
   const CGState *st;
-  const void *r;
+  void *r;
+  void *x;
   void *p;
   void *Ap;
   double *partial;
   unsigned char td[sizeof(TangentData<double>)];
 };
+template <typename R> struct BatchVec;
 template <typename R>
-int cg_operator_batch(Spectral &sp, int tkind, const ProblemPtrs<R> *tab, int B, cudaStream_t s);
+int cg_operator_batch(Spectral &sp, int tkind, const ProblemPtrs<R> *tab, const BatchVec<R> *xtab, int B,
+                      cudaStream_t s);
 // Times candidate launch shapes of each pass on this grid (CUDA events) and keeps
 // the fastest (FFT_PlanFlags::measure / patient); fp32 selects the FP32 passes.
 template <typename R> void spectral_autotune(Spectral &sp, cudaStream_t s, int effort);
@@ -262,6 +270,13 @@ template <typename R> struct BatchVec {
 };
 template <typename R>
 void cg_update_batch(const BatchVec<R> *tab, long long n, int B, cudaStream_t s);
+// alpha from the forward pass's nparts block sums of p.(K:p) and x += alpha p of the
+// FP32 inner solve's iteration, launched between its forward and inverse passes
+// (solo / batched; a batch's problems have nparts sums each in their partial arrays)
+template <typename R>
+void cg_update_x(const CGState *st, R *x, const R *p, long long n, const double *partial, int nparts,
+                 cudaStream_t s);
+template <typename R> void cg_update_x_batch(const BatchVec<R> *tab, long long n, int nparts, int B, cudaStream_t s);
 // FP64 dot of a with b over n entries into *out_device (deterministic)
 template <typename Ra, typename Rb>
 void dot_device(const Ra *a, const Rb *b, long long n, double *partial, double *out,
@@ -318,6 +333,9 @@ void aos_to_soa(const double *aos, double *soa, int ncomp, long long npx, cudaSt
 void soa_to_aos(const double *soa, double *aos, int ncomp, long long npx, cudaStream_t s);
 void soa_to_aos_complex(const double2 *soa, double2 *aos, int ncomp, long long nk, cudaStream_t s);
 void aos_to_soa_complex(const double2 *aos, double2 *soa, int ncomp, long long nk, cudaStream_t s);
+
+// measured FP64 FMA throughput of the current device, TFLOP/s (probe.cu)
+double fp64_fma_tflops(cudaStream_t s);
 
 // allocation-free projection on caller device buffers (noalloc.cu)
 void noalloc_project(int dim, const int *resolutions, const double *lengths, int kind, int flags,

@@ -3,9 +3,10 @@
 // or with same-shape requests by musg_batch_newton_cg.
 //
 // Admission: a lane takes the oldest waiting request whose device footprint fits the
-// HBM budget next to the requests already running (an idle server takes any
-// request, so one larger than the budget still runs, alone), plus the waiting
-// requests of the same shape that fit too, up to max_batch.  Lanes are host threads,
+// HBM budget next to the requests already running (a request larger than the whole
+// budget is refused at submission), plus the waiting requests of the same shape that
+// fit too, up to max_batch (requests with the consistent elasto-plastic tangent run
+// alone, with newton_cg's line search).  Lanes are host threads,
 // each with its own non-blocking CUDA stream, so admitted groups overlap on the
 // device.  A group's memory returns to the budget when it completes.  Latency is
 // measured from submission to completion on the host's steady clock.
@@ -46,12 +47,13 @@ struct Req {
   std::vector<unsigned char> phase;
   long long npx = 0;
   bool has_hep = false, any_le = false, has_le2 = false;
+  bool has_full = false;  // an HEP1 material with the consistent tangent (D^4 tangent planes)
   unsigned long long bytes = 0;
   std::tuple<int, int, int, int, int, int, int, int, int, int, int> key;
   Clock::time_point t0;
 };
 
-unsigned long long footprint(int dim, const int *res, int form, bool has_hep, int precision) {
+unsigned long long footprint(int dim, const int *res, int form, bool has_hep, bool has_full, int precision) {
   unsigned long long npx = 1;
   for (int d = 0; d < dim; ++d) npx *= (unsigned long long)res[d];
   const unsigned long long d2 = (unsigned long long)dim * dim;
@@ -61,11 +63,13 @@ unsigned long long footprint(int dim, const int *res, int form, bool has_hep, in
   // index + lambda/mu, and 1 MiB of plans and reduction scratch
   unsigned long long b = 3 * d2 * npx * 8 + d2 * nk * 16 + 2 * d2 * npx * 8 + npx * (1 + 16) + (1ull << 20);
   if (form == MUSG_FINITE_STRAIN) b += 2 * d2 * npx * 8;  // S and F of the tangent
-  if (has_hep) b += 38 * npx * 8 + d2 * dim * npx * 8;    // plastic state, K'
+  if (has_hep) b += 38 * npx * 8;                          // plastic state
+  const unsigned long long tplanes = has_full ? d2 * d2 : has_hep ? d2 * dim : 0;  // K or K'
+  b += tplanes * npx * 8;
   if (precision == MUSG_PRECISION_MIXED) {
-    b += npx * 8 + d2 * nk * 8 + 4 * d2 * npx * 4;  // FP32 lambda/mu, spectrum, CG vectors
+    b += npx * 8 + d2 * nk * 8 + 3 * d2 * npx * 4;  // FP32 lambda/mu, spectrum, CG vectors x r p
     if (form == MUSG_FINITE_STRAIN) b += 2 * d2 * npx * 4;
-    if (has_hep) b += d2 * dim * npx * 4;
+    b += tplanes * npx * 4;
   } else {
     b += 4 * d2 * npx * 8;  // FP64 CG vectors
   }
@@ -120,17 +124,21 @@ std::shared_ptr<Req> copy_request(const musg_request &src, int precision) {
   if (!need_pp) q->r.per_pixel_stride = 0;
   q->r.load_steps = q->steps.data();
   for (int m = 0; m < src.nb_materials; ++m) {
-    if (q->laws[m] == MUSG_LAW_HEP1) q->has_hep = true;
-    else q->any_le = true;
+    if (q->laws[m] == MUSG_LAW_HEP1) {
+      q->has_hep = true;
+      q->has_full |= (int)q->params[5 * m + 4] == kHep1Consistent;
+    } else {
+      q->any_le = true;
+    }
   }
   need(!(q->has_hep && src.formulation == MUSG_SMALL_STRAIN), MUSG_ERR_ARGUMENT,
        "MaterialHyperElastoPlastic1 needs the finite-strain formulation");
   int res[3] = {1, 1, 1};
   for (int d = 0; d < src.dim; ++d) res[d] = src.resolutions[d];
-  q->bytes = footprint(src.dim, res, src.formulation, q->has_hep, precision);
+  q->bytes = footprint(src.dim, res, src.formulation, q->has_hep, q->has_full, precision);
   // same shape = same grid, formulation, flags, number of steps and tangent kind
   q->key = std::make_tuple(src.dim, res[0], res[1], res[2], src.formulation, src.flags, src.nb_steps,
-                           (int)q->has_hep, (int)q->any_le, (int)q->has_le2, 0);
+                           (int)q->has_hep, (int)q->any_le, (int)q->has_le2, (int)q->has_full);
   return q;
 }
 
@@ -194,10 +202,11 @@ struct musg_server {
     used = 0;
     for (size_t i = 0; i < queue.size(); ++i) {
       const auto &q = queue[i];
-      if (in_use + q->bytes > budget && in_use > 0) continue;
+      if (in_use + q->bytes > budget) continue;
       group.push_back(q);
       used = q->bytes;
-      for (size_t k = i + 1; k < queue.size() && (int)group.size() < max_batch; ++k) {
+      // requests solved with the line search (consistent elasto-plastic tangent) run alone
+      for (size_t k = i + 1; k < queue.size() && (int)group.size() < max_batch && !q->has_full; ++k) {
         const auto &o = queue[k];
         if (o->key == q->key && in_use + used + o->bytes <= budget) {
           group.push_back(o);
@@ -237,6 +246,8 @@ struct musg_server {
         musg_solver *sv = nullptr;
         if (musg_solver_cg_create(cells[0], tol, maxiter, 0, precision, &sv) != MUSG_OK)
           throw Error(MUSG_ERR_RUNTIME, musg_last_error());
+        // the consistent elasto-plastic tangent converges with the line search
+        musg_solver_set_line_search(sv, group[0]->has_full ? 1 : 0);
         rc[0] = musg_newton_cg(cells[0], group[0]->steps.data(), ns, sv, newton_tol, 0.0, 0, infos.data(), nullptr,
                                nullptr);
         if (rc[0] != MUSG_OK) err[0] = musg_last_error();
@@ -335,7 +346,10 @@ int musg_request_bytes(const musg_request *req, int precision, unsigned long lon
     check_request(*req);
     int res[3] = {1, 1, 1};
     for (int d = 0; d < req->dim; ++d) res[d] = req->resolutions[d];
-    *bytes = footprint(req->dim, res, req->formulation, has_law(*req, MUSG_LAW_HEP1), precision);
+    bool full = false;
+    for (int m = 0; m < req->nb_materials; ++m)
+      full |= req->laws[m] == MUSG_LAW_HEP1 && req->params && (int)req->params[5 * m + 4] == kHep1Consistent;
+    *bytes = footprint(req->dim, res, req->formulation, has_law(*req, MUSG_LAW_HEP1), full, precision);
   });
 }
 
@@ -367,6 +381,11 @@ int musg_server_submit(musg_server *srv, const musg_request *req, long long *id)
   return guarded([&] {
     need(srv && req, MUSG_ERR_ARGUMENT, "null argument");
     auto q = copy_request(*req, srv->precision);
+    // a request that cannot fit the budget even on an idle server is refused here,
+    // instead of being admitted alone and overcommitting the device
+    if (q->bytes > srv->budget)
+      throw Error(MUSG_ERR_MEMORY, "request needs " + std::to_string(q->bytes) + " bytes of device memory, above the "
+                                       "server's HBM budget of " + std::to_string(srv->budget) + " bytes");
     {
       std::lock_guard<std::mutex> lk(srv->mu);
       need(!srv->closed, MUSG_ERR_RUNTIME, "the server is closed");

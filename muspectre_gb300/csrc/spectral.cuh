@@ -24,8 +24,19 @@
 
 namespace musg {
 
-enum Prologue : int { PRO_PLAIN = 0, PRO_TANGENT = 1, PRO_CG = 2 };
-enum Epilogue : int { EPI_PLAIN = 0, EPI_CG = 1 };
+// PRO_CG / EPI_CG: the reference's CG iteration (solver_cg.cc:76-97) split over the
+// passes: the last pass writes Ap and finishes alpha = r.r / p.Ap, and cg_update then
+// applies x += alpha p, r += alpha Ap and finishes beta.  PRO_CGF / EPI_CGF (the FP32
+// inner solve of the mixed-precision path): p stays in the range of the projection
+// G (x0 = 0, rhs = G(-P)), and G is self-adjoint and idempotent, so p.Ap =
+// p.G(K:p) = p.(K:p); the forward pass forms K:p per pixel anyway and writes per-warp
+// sums of p.(K:p) (no block barrier, ticket or memory fence in its many short blocks),
+// cg_alpha finishes alpha in one block, and cg_update_x applies x += alpha p.  The
+// inverse pass applies r += alpha Ap straight from its registers and finishes beta,
+// so Ap is never stored: per iteration the field traffic drops from 19 to 16
+// field-sized passes plus the tangent data.
+enum Prologue : int { PRO_PLAIN = 0, PRO_TANGENT = 1, PRO_CG = 2, PRO_CGF = 3 };
+enum Epilogue : int { EPI_PLAIN = 0, EPI_CG = 1, EPI_CGF = 2 };
 enum GreenMode : int { GM_SMALL = 0, GM_FINITE = 1, GM_FWD = 2, GM_INV = 3 };
 
 // independent global loads each thread keeps in flight in the staging loops
@@ -78,6 +89,23 @@ __device__ __forceinline__ double block_sum(double v) {
   }
   return v;
 }
+
+// sum of v over the calling warp, written by its first lane to out[w] (w = the warp's
+// index in the block); a partial last warp shuffles among its existing lanes only.
+// No block barrier: for the per-warp partial sums of short-lived blocks.
+__device__ __forceinline__ void warp_partial(double v, double *out) {
+  const int nth = blockDim.x * blockDim.y * blockDim.z;
+  const int tid = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
+  const int w = tid >> 5, l = tid & 31;
+  const int nl = min(32, nth - (w << 5));
+  const unsigned mask = nl == 32 ? 0xffffffffu : ((1u << nl) - 1u);
+  for (int o = 16; o > 0; o >>= 1) {
+    const double t = __shfl_down_sync(mask, v, o);
+    if (l + o < nl) v += t;
+  }
+  if (l == 0) out[w] = v;
+}
+__device__ __forceinline__ int warps_per_block() { return (blockDim.x * blockDim.y * blockDim.z + 31) >> 5; }
 
 // ------------------------------------------------------------ CG scalar steps
 // The kernel that produces a dot product's partial sums also finishes it: every block
@@ -365,7 +393,8 @@ template <int D, int TK, typename R> struct TangentLocal {
 template <typename R> struct ProblemPtrs {
   typename V2<R>::T *spec;
   const CGState *st;
-  const R *r;
+  R *r;
+  R *x;
   R *p;
   R *Ap;
   double *partial;
@@ -381,9 +410,10 @@ template <typename R> struct LastArgs {
   R *out;
   R scale;
   const CGState *st;
-  const R *r;
+  R *r;
+  R *x;   // the CG iterate (not read by the pass kernels; kept with the problem's pointers)
   R *p;
-  R *Ap;
+  R *Ap;  // EPI_CGF: stored only when set (operator checks)
   double *partial;
   TangentData<R> td;
   const ProblemPtrs<R> *batch;  // null: a single problem
@@ -393,6 +423,7 @@ template <typename R> struct LastArgs {
     spec = q.spec;
     st = q.st;
     r = q.r;
+    x = q.x;
     p = q.p;
     Ap = q.Ap;
     partial = q.partial;
@@ -410,8 +441,10 @@ __global__ void __launch_bounds__(kPassThreads) k_last_fwd(const LastArgs<R> a0)
   a.bind();
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T *buf = reinterpret_cast<T *>(smem_raw);
-  if (PRO == PRO_CG && !a.st->active) return;
+  constexpr bool kCG = PRO == PRO_CG || PRO == PRO_CGF;
+  if (kCG && !a.st->active) return;
   const int L = a.L, G = a.G, nc = a.ncomp, G2 = G >> 1;
+  Acc<R> pkp;  // PRO_CGF: partial sum of p.(K:p)
   const int P = nc * G2;
   T *buf2 = buf + (size_t)P * a.ap.m;
   const long long row0 = (long long)blockIdx.x * G;
@@ -442,8 +475,8 @@ __global__ void __launch_bounds__(kPassThreads) k_last_fwd(const LastArgs<R> a0)
     }
   } else {
     constexpr int D2 = D * D;
-    const bool first = (PRO == PRO_CG) ? (a.st->iter == 0) : false;
-    const R beta = (PRO == PRO_CG) ? R(a.st->beta) : R(0);
+    const bool first = kCG ? (a.st->iter == 0) : false;
+    const R beta = kCG ? R(a.st->beta) : R(0);
     for (int idx = threadIdx.x; idx < G * L; idx += blockDim.x) {
       int e;
       const int g = fL.div(idx, e);
@@ -453,7 +486,7 @@ __global__ void __launch_bounds__(kPassThreads) k_last_fwd(const LastArgs<R> a0)
         const long long px = row * L + e;
         R v[D2];
         TangentLocal<D, TK, R> tl;
-        if (PRO == PRO_CG) {
+        if (kCG) {
           R rv[D2], pv[D2];
 #pragma unroll
           for (int c = 0; c < D2; ++c) {
@@ -473,6 +506,12 @@ __global__ void __launch_bounds__(kPassThreads) k_last_fwd(const LastArgs<R> a0)
           tl.load(a.td, px, a.npx);
         }
         tl.apply(v, out);
+        if (PRO == PRO_CGF) {
+          R q = R(0);  // p.(K:p) of the pixel, then one compensated add
+#pragma unroll
+          for (int c = 0; c < D2; ++c) q += v[c] * out[c];
+          pkp.add(q);
+        }
       } else {
 #pragma unroll
         for (int c = 0; c < D2; ++c) out[c] = R(0);
@@ -500,6 +539,7 @@ __global__ void __launch_bounds__(kPassThreads) k_last_fwd(const LastArgs<R> a0)
     else o = T{R(0.5) * (z.y + zn.y), R(-0.5) * (z.x - zn.x)};
     a.spec[(long long)c * a.nk + row * H + k] = o;
   }
+  if constexpr (PRO == PRO_CGF) warp_partial(pkp.value(), a.partial + (size_t)blockIdx.x * warps_per_block());
 }
 
 // inverse: half spectra -> real rows.  PLAIN writes out = scale*x; CG writes Ap
@@ -512,7 +552,7 @@ __global__ void __launch_bounds__(kPassThreads) k_last_inv(const LastArgs<R> a0)
   a.bind();
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T *buf = reinterpret_cast<T *>(smem_raw);
-  if (EPI == EPI_CG && !a.st->active) return;
+  if (EPI != EPI_PLAIN && !a.st->active) return;
   const int L = a.L, G = a.G, nc = a.ncomp, G2 = G >> 1, H = a.H;
   const int P = nc * G2;
   T *buf2 = buf + (size_t)P * a.ap.m;
@@ -564,24 +604,37 @@ __global__ void __launch_bounds__(kPassThreads) k_last_inv(const LastArgs<R> a0)
   } else {
     constexpr int D2 = D * D;
     Acc<R> acc;
+    const R alpha = EPI == EPI_CGF ? R(a.st->alpha) : R(0);
     for (int idx = threadIdx.x; idx < G * L; idx += blockDim.x) {
       int e;
       const int g = fL.div(idx, e);
       const long long row = row0 + g;
       if (row >= a.nrows) continue;
       const long long px = row * L + e;
+      R q = R(0);
 #pragma unroll
       for (int c = 0; c < D2; ++c) {
         const R v = bufr[2 * (e * P + c * G2 + (g >> 1)) + (g & 1)];
         const long long o = (long long)c * a.npx + px;
-        a.Ap[o] = v;
-        acc.add(a.p[o] * v);
+        if constexpr (EPI == EPI_CG) {
+          a.Ap[o] = v;
+          acc.add(a.p[o] * v);
+        } else {
+          if (a.Ap) a.Ap[o] = v;
+          const R rn = a.r[o] + alpha * v;
+          a.r[o] = rn;
+          q += rn * rn;
+        }
       }
+      if constexpr (EPI == EPI_CGF) acc.add(q);
     }
     const double bs = block_sum(acc.value());
     if (threadIdx.x == 0) a.partial[blockIdx.x] = bs;
     CGState *st = const_cast<CGState *>(a.st);
-    if (cg_last_block(st)) cg_alpha_step(st, a.partial, gridDim.x);
+    if (cg_last_block(st)) {
+      if constexpr (EPI == EPI_CG) cg_alpha_step(st, a.partial, gridDim.x);
+      else cg_beta_step(st, a.partial, gridDim.x);
+    }
   }
 }
 

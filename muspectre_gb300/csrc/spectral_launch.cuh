@@ -291,10 +291,11 @@ int last_cg_reg(Spectral &sp, int tkind, LastArgs<R> a, int G, bool inv, cudaStr
     const long ps = m + m / RegLanesR1(m);
     a.G = G;
     const dim3 grid(blocks, B), block(Y, nc * G2);
+    const int wpb = (Y * nc * G2 + 31) / 32;  // warps per block (the forward pass's partial sums per block)
     const size_t smem = ((size_t)nc * G2 * ps + m) * sizeof(float2);  // pencils + twiddle table
     if (!inv) {
 #define MUSG_FR(DD, TT) \
-  if (sp.g.dim == DD && tkind == TT) { launch_fwd_reg<DD, TT>(m, a, grid, block, smem, s); return blocks; }
+  if (sp.g.dim == DD && tkind == TT) { launch_fwd_reg<DD, TT>(m, a, grid, block, smem, s); return blocks * wpb; }
       MUSG_FR(2, TK_SMALL) MUSG_FR(2, TK_FINITE) MUSG_FR(2, TK_KPRIME) MUSG_FR(2, TK_MIXED) MUSG_FR(2, TK_FISO)
       MUSG_FR(3, TK_SMALL) MUSG_FR(3, TK_FINITE) MUSG_FR(3, TK_KPRIME) MUSG_FR(3, TK_MIXED) MUSG_FR(3, TK_FISO)
       MUSG_FR(2, TK_GSMALL) MUSG_FR(2, TK_GFINITE) MUSG_FR(3, TK_GSMALL) MUSG_FR(3, TK_GFINITE)
@@ -473,13 +474,17 @@ void spectral_project(Spectral &sp, const R *in, R *out, R in_scale, cudaStream_
 }
 
 template <typename R>
-int cg_operator(Spectral &sp, int tkind, const TangentData<R> &td, const CGState *st, const R *r, R *p,
+int cg_operator(Spectral &sp, int tkind, const TangentData<R> &td, const CGState *st, R *r, R *x, R *p,
                 R *Ap, double *partial, cudaStream_t s, cudaEvent_t *ev) {
+  // FP32 (the mixed path's inner solve): the fused iteration; FP64: the reference's
+  constexpr int kPro = sizeof(R) == 4 ? PRO_CGF : PRO_CG;
+  constexpr int kEpi = sizeof(R) == 4 ? EPI_CGF : EPI_CG;
   const int gm = green_mode_of(sp);
   const Cfg c = last_cfg<R>(sp);
   LastArgs<R> a = last_args<R>(sp, c);
   a.st = st;
   a.r = r;
+  a.x = x;
   a.p = p;
   a.Ap = Ap;
   a.partial = partial;
@@ -491,9 +496,15 @@ int cg_operator(Spectral &sp, int tkind, const TangentData<R> &td, const CGState
   const int gfwd = last_reg_rows<R>(sp, false), ginv = last_reg_rows<R>(sp, true);
   const bool greg = gfwd && ginv;
   mark();
-  if (greg) last_cg_reg<R>(sp, tkind, a, gfwd, false, s, 1);
-  else dispatch_fwd<R, PRO_CG>(sp.g.dim, tkind, a, c, s);
+  int nfwd = c.blocks * ((c.threads + 31) / 32);  // the forward pass's per-warp partial sums
+  if (greg) nfwd = last_cg_reg<R>(sp, tkind, a, gfwd, false, s, 1);
+  else dispatch_fwd<R, kPro>(sp.g.dim, tkind, a, c, s);
   mark();
+  if constexpr (sizeof(R) == 4) {
+    // alpha, and x += alpha p, between the forward pass and the one that may end the loop
+    cg_update_x<R>(st, x, p, sp.g.npx * sp.ncomp, partial, nfwd, s);
+    mark();
+  }
   if (sp.g.dim == 3) {
     run_axis<R>(sp, false, st, s);
     mark();
@@ -509,8 +520,8 @@ int cg_operator(Spectral &sp, int tkind, const TangentData<R> &td, const CGState
     mark();
     return nb;
   }
-  if (sp.g.dim == 2) launch_inv<R, EPI_CG, 2>(a, c, s);
-  else launch_inv<R, EPI_CG, 3>(a, c, s);
+  if (sp.g.dim == 2) launch_inv<R, kEpi, 2>(a, c, s);
+  else launch_inv<R, kEpi, 3>(a, c, s);
   mark();
   return c.blocks;
 }
@@ -520,21 +531,26 @@ static_assert(sizeof(ProblemPtrs<float>) == sizeof(ProblemPtrsHost) &&
               "host image of the batch table");
 
 template <typename R>
-int cg_operator_batch(Spectral &sp, int tkind, const ProblemPtrs<R> *tab, int B, cudaStream_t s) {
+int cg_operator_batch(Spectral &sp, int tkind, const ProblemPtrs<R> *tab, const BatchVec<R> *xtab, int B,
+                      cudaStream_t s) {
+  constexpr int kPro = sizeof(R) == 4 ? PRO_CGF : PRO_CG;
+  constexpr int kEpi = sizeof(R) == 4 ? EPI_CGF : EPI_CG;
   const int gm = green_mode_of(sp);
   const Cfg c = last_cfg<R>(sp);
   LastArgs<R> a = last_args<R>(sp, c);
   a.batch = tab;
   const int gfwd = last_reg_rows<R>(sp, false), ginv = last_reg_rows<R>(sp, true);
   const bool greg = gfwd && ginv;
-  if (greg) last_cg_reg<R>(sp, tkind, a, gfwd, false, s, B);
-  else dispatch_fwd<R, PRO_CG>(sp.g.dim, tkind, a, c, s, B);
+  int nfwd = c.blocks * ((c.threads + 31) / 32);
+  if (greg) nfwd = last_cg_reg<R>(sp, tkind, a, gfwd, false, s, B);
+  else dispatch_fwd<R, kPro>(sp.g.dim, tkind, a, c, s, B);
+  if constexpr (sizeof(R) == 4) cg_update_x_batch<R>(xtab, sp.g.npx * sp.ncomp, nfwd, B, s);
   if (sp.g.dim == 3) run_axis<R>(sp, false, nullptr, s, tab, B);
   run_green<R>(sp, gm, nullptr, s, tab, B);
   if (sp.g.dim == 3) run_axis<R>(sp, true, nullptr, s, tab, B);
   if (greg) return last_cg_reg<R>(sp, tkind, a, ginv, true, s, B);
-  if (sp.g.dim == 2) launch_inv<R, EPI_CG, 2>(a, c, s, B);
-  else launch_inv<R, EPI_CG, 3>(a, c, s, B);
+  if (sp.g.dim == 2) launch_inv<R, kEpi, 2>(a, c, s, B);
+  else launch_inv<R, kEpi, 3>(a, c, s, B);
   return c.blocks;
 }
 
@@ -637,11 +653,12 @@ template <typename R> void spectral_autotune(Spectral &sp, cudaStream_t s, int e
   template void spectral_forward<R>(Spectral &, const R *, R, cudaStream_t);                      \
   template void spectral_inverse<R>(Spectral &, R *, R, cudaStream_t);                            \
   template void spectral_project<R>(Spectral &, const R *, R *, R, cudaStream_t);                 \
-  template int cg_operator<R>(Spectral &, int, const TangentData<R> &, const CGState *, const R *, \
+  template int cg_operator<R>(Spectral &, int, const TangentData<R> &, const CGState *, R *, R *,  \
                               R *, R *, double *, cudaStream_t, cudaEvent_t *);                    \
   template void tangent_operator<R>(Spectral &, int, const TangentData<R> &, const R *, R *,       \
                                     cudaStream_t);                                                 \
   template void spectral_autotune<R>(Spectral &, cudaStream_t, int);                               \
-  template int cg_operator_batch<R>(Spectral &, int, const ProblemPtrs<R> *, int, cudaStream_t);
+  template int cg_operator_batch<R>(Spectral &, int, const ProblemPtrs<R> *, const BatchVec<R> *, int,         \
+                                    cudaStream_t);
 
 }  // namespace musg

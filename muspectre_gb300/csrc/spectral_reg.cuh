@@ -261,8 +261,9 @@ template <int M> struct LastLayout {
   static __device__ __forceinline__ int pos(int s) { return s + s / R1; }
 };
 
-// forward with the CG prologue: p = -r + beta p (p = -r on the first iteration),
-// v = K:p per pixel, spectrum of v.  FP32 only.
+// forward with the CG prologue of the FP32 inner solve (PRO_CGF): p = -r + beta p
+// (p = -r on the first iteration), v = K:p per pixel, spectrum of v, and the per-warp
+// sums of p.v (cg_alpha finishes alpha = r.r / p.(K:p) from them).  FP32 only.
 template <int M, int D, int TK>
 __global__ void __launch_bounds__(512) k_last_fwd_reg(const LastArgs<float> a0) {
   dep_wait();
@@ -285,6 +286,7 @@ __global__ void __launch_bounds__(512) k_last_fwd_reg(const LastArgs<float> a0) 
   const long long row0 = (long long)blockIdx.x * G;
   const bool first = a.st->iter == 0;
   const R beta = R(a.st->beta);
+  Acc<R> pkp;
   for (int idx = tid; idx < G * L; idx += nth) {
     const int g = idx / L, e = idx % L;  // L is a power of two
     const long long row = row0 + g;
@@ -306,6 +308,10 @@ __global__ void __launch_bounds__(512) k_last_fwd_reg(const LastArgs<float> a0) 
         a.p[(long long)c * a.npx + px] = v[c];
       }
       tl.apply(v, out);
+      R q = R(0);  // p.(K:p) of the pixel, then one compensated add
+#pragma unroll
+      for (int c = 0; c < D2; ++c) q += v[c] * out[c];
+      pkp.add(q);
     } else {
 #pragma unroll
       for (int c = 0; c < D2; ++c) out[c] = R(0);
@@ -347,12 +353,35 @@ __global__ void __launch_bounds__(512) k_last_fwd_reg(const LastArgs<float> a0) 
     if (rx < a.nrows) sx[k] = T{R(0.5) * (z.x + zn.x), R(0.5) * (z.y - zn.y)};
     if (ry < a.nrows) sx[H + k] = T{R(0.5) * (z.y + zn.y), R(-0.5) * (z.x - zn.x)};
   }
+  warp_partial(pkp.value(), a.partial + (size_t)blockIdx.x * warps_per_block());
 }
 
-// inverse with the CG epilogue: Ap = real rows of the spectrum, partial[block] = sum
-// of p.Ap over the block's rows.  The p entries of a lane's outputs are loaded before
-// the transform, after its spectrum entries, so that they are in flight with the
-// transform.  FP32 only.
+// the epilogue of the FP32 inner solve's inverse pass (EPI_CGF) for the entries o of
+// rows x and y of a lane (ok: the row exists): Ap = v (stored only for operator
+// checks), r += alpha Ap; returns the new r.r of the two entries
+__device__ __forceinline__ float cgf_pair(const LastArgs<float> &a, long long ox, long long oy, bool okx, bool oky,
+                                          float alpha, float rx, float ry, float2 v) {
+  float q = 0.f;
+  if (okx) {
+    if (a.Ap) a.Ap[ox] = v.x;
+    const float rn = rx + alpha * v.x;
+    a.r[ox] = rn;
+    q += rn * rn;
+  }
+  if (oky) {
+    if (a.Ap) a.Ap[oy] = v.y;
+    const float rn = ry + alpha * v.y;
+    a.r[oy] = rn;
+    q += rn * rn;
+  }
+  return q;
+}
+
+// inverse with the CG epilogue of the FP32 inner solve (EPI_CGF): c2r of the rows,
+// r += alpha Ap, partial[block] = sum of the new r.r over the block's rows, and the
+// last block to finish sets beta and the loop condition.  The r entries of a lane's
+// outputs are loaded before the transform, after its spectrum entries, so that they
+// are in flight with the transform.  FP32 only.
 template <int M, int D>
 __global__ void __launch_bounds__(384, 2) k_last_inv_reg(const LastArgs<float> a0) {
   dep_wait();
@@ -401,11 +430,11 @@ __global__ void __launch_bounds__(384, 2) k_last_inv_reg(const LastArgs<float> a
       w[b][r] = T{x.x - z.y, x.y + z.x};
     }
   }
-  R px[F::R1], py[F::R1];
+  R px[F::R1], py[F::R1];  // the r entries of the lane's outputs
 #pragma unroll
   for (int r = 0; r < F::R1; ++r) {
-    px[r] = okx ? a.p[ox + y + F::Y * r] : R(0);
-    py[r] = oky ? a.p[oy + y + F::Y * r] : R(0);
+    px[r] = okx ? a.r[ox + y + F::Y * r] : R(0);
+    py[r] = oky ? a.r[oy + y + F::Y * r] : R(0);
   }
   __syncthreads();  // the twiddle copy
 #pragma unroll
@@ -423,22 +452,16 @@ __global__ void __launch_bounds__(384, 2) k_last_inv_reg(const LastArgs<float> a
   for (int r = 0; r < F::R1; ++r) v[r] = col[Lay::pos(y * F::R1 + r)];
   Dft<F::R1, true, T>::run(v);
   Acc<R> acc;
+  const R alpha = R(a.st->alpha);
 #pragma unroll
   for (int r = 0; r < F::R1; ++r) {
     const int e = y + F::Y * r;
-    if (okx) {
-      a.Ap[ox + e] = v[r].x;
-      acc.add(px[r] * v[r].x);
-    }
-    if (oky) {
-      a.Ap[oy + e] = v[r].y;
-      acc.add(py[r] * v[r].y);
-    }
+    acc.add(cgf_pair(a, ox + e, oy + e, okx, oky, alpha, px[r], py[r], v[r]));
   }
   const double bs = block_sum(acc.value());
   if (y == 0 && q == 0) a.partial[blockIdx.x] = bs;
   CGState *st = const_cast<CGState *>(a.st);
-  if (cg_last_block(st)) cg_alpha_step(st, a.partial, gridDim.x);
+  if (cg_last_block(st)) cg_beta_step(st, a.partial, gridDim.x);
 }
 
 }  // namespace musg

@@ -295,15 +295,16 @@ __device__ __forceinline__ void bulk_load(void *dst, const void *src, uint32_t b
       : "memory");
 }
 
-// Last-axis inverse with the CG epilogue (the pass k_last_inv_reg computes), fed by
+// Last-axis inverse with the CG epilogue (the pass k_last_inv_reg computes: r += alpha Ap,
+// new r.r), fed by
 // bulk copies: a persistent block walks tiles of G rows; one thread stages the next
 // tile's half spectra (per component the G rows are G*H contiguous complex values: one
 // cp.async.bulk of G*H*8 bytes each) while the block transforms the current tile.  A
 // lane reads all its spectrum entries of the tile into registers first, so after one
 // barrier the tile's stage doubles as the transform's exchange buffer and a block
-// needs two stages only.  The p entries are loaded from global memory at the start of
-// each tile (they are needed in the epilogue).  Each block sums p.Ap over its tiles
-// into one partial sum; the last block to finish computes alpha.  A batched launch
+// needs two stages only.  The r entries are loaded from global memory at the start of
+// each tile (they are needed in the epilogue).  Each block sums the new r.r over its
+// tiles into one partial sum; the last block to finish sets beta.  A batched launch
 // (a.batch) runs problem blockIdx.y with its own pointers, state and partial sums, in
 // the same order as a single-problem launch, so batched and solo results agree bit for
 // bit.  Dynamic shared memory: k_last_inv_tma_smem bytes.
@@ -374,6 +375,7 @@ __global__ void __maxnreg__(96) k_last_inv_tma(const LastArgs<float> a0, unsigne
     }
   }
   Acc<R> acc;
+  const R alpha = R(a.st->alpha);
   for (int it = 0; tile < ntiles; ++it, tile += gridDim.x) {
     const int s = it & 1;
     const uint32_t parity = (uint32_t)((it >> 1) & 1);
@@ -381,11 +383,11 @@ __global__ void __maxnreg__(96) k_last_inv_tma(const LastArgs<float> a0, unsigne
     const long long rx = row0 + 2 * g2, ry = rx + 1;
     const bool okx = rx < a.nrows, oky = ry < a.nrows;
     const long long ox = (long long)c * a.npx + rx * L, oy = ox + L;
-    R px[F::R1], py[F::R1];
+    R px[F::R1], py[F::R1];  // the r entries of the lane's outputs
 #pragma unroll
     for (int r = 0; r < F::R1; ++r) {
-      px[r] = okx ? a.p[ox + y + F::Y * r] : R(0);
-      py[r] = oky ? a.p[oy + y + F::Y * r] : R(0);
+      px[r] = okx ? a.r[ox + y + F::Y * r] : R(0);
+      py[r] = oky ? a.r[oy + y + F::Y * r] : R(0);
     }
     if (tid == 0) {
       if (mbar_wait_bounded(&bars[s], parity)) {
@@ -457,20 +459,13 @@ __global__ void __maxnreg__(96) k_last_inv_tma(const LastArgs<float> a0, unsigne
 #pragma unroll
     for (int r = 0; r < F::R1; ++r) {
       const int e = y + F::Y * r;
-      if (okx) {
-        a.Ap[ox + e] = v[r].x;
-        acc.add(px[r] * v[r].x);
-      }
-      if (oky) {
-        a.Ap[oy + e] = v[r].y;
-        acc.add(py[r] * v[r].y);
-      }
+      acc.add(cgf_pair(a, ox + e, oy + e, okx, oky, alpha, px[r], py[r], v[r]));
     }
   }
   const double bs = block_sum(acc.value());
   if (tid == 0) a.partial[blockIdx.x] = bs;
   CGState *st = const_cast<CGState *>(a.st);
-  if (cg_last_block(st)) cg_alpha_step(st, a.partial, gridDim.x);
+  if (cg_last_block(st)) cg_beta_step(st, a.partial, gridDim.x);
 }
 
 }  // namespace musg

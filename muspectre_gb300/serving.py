@@ -98,9 +98,10 @@ def _native(req):
     return r, (laws, params, phase, per_pixel, steps)
 
 
-def estimate_bytes(res, formulation, has_hep, precision='mixed'):
+def estimate_bytes(res, formulation, has_hep, precision='mixed', consistent=False):
     """Device memory of one admitted request (fields, spectra, tangent data, CG
-    vectors, state), as the library allocates it (musg_request_bytes)."""
+    vectors, state), as the library allocates it (musg_request_bytes);
+    ``consistent``: its elasto-plastic material has the consistent tangent."""
     r = L.Request()
     r.dim = len(res)
     for i, n in enumerate(res):
@@ -109,6 +110,8 @@ def estimate_bytes(res, formulation, has_hep, precision='mixed'):
     r.nb_materials = 1
     law = (C.c_int * 1)(L.LAW_HEP1 if has_hep else L.LAW_LE1)
     r.laws = C.cast(law, C.POINTER(C.c_int))
+    prm = (C.c_double * 5)(0, 0, 0, 0, 2.0 if consistent else 0.0)
+    r.params = C.cast(prm, C.POINTER(C.c_double))
     out = C.c_ulonglong(0)
     L.check(L.lib().musg_request_bytes(C.byref(r), _PREC[precision], C.byref(out)))
     return int(out.value)
@@ -219,8 +222,9 @@ def solve_alone(req, tol=1e-8, maxiter=2000, newton_tol=1e-6, precision='mixed')
 def c5_request(rid, seed, small=False):
     """A request of the mixed serving stream, drawn from its own seed: 2-D (64..1024, 2/3/5-smooth)
     or 3-D (32..160, 2/3/5-smooth); small or finite strain; LE1/LE4, or HEP1 with 1-10
-    load steps (finite strain only); 1-60 spheres; E ~ U[1e9, 300e9], nu ~ U[0.2, 0.4];
-    symmetric macro strain entries ~ U[-0.02, 0.02].  ``small`` caps the sizes (tests)."""
+    load steps (finite strain only; the consistent tangent, so that heterogeneous
+    cells converge); 1-60 spheres; E ~ U[1e9, 300e9], nu ~ U[0.2, 0.4]; symmetric
+    macro strain entries ~ U[-0.02, 0.02].  ``small`` caps the sizes (tests)."""
     rng = np.random.default_rng(seed)
     smooth = lambda lo, hi: [n for n in range(lo, hi + 1) if _smooth235(n)]
     d = 2 if rng.random() < 0.5 else 3
@@ -233,20 +237,29 @@ def c5_request(rid, seed, small=False):
     hep = rng.random() < 0.2
     form = Formulation.finite_strain if (hep or rng.random() < 0.5) else Formulation.small_strain
     nsph = int(rng.integers(1, 61))
-    pts = np.stack(np.meshgrid(*[np.arange(n)] * d, indexing='ij'), -1).reshape(-1, d).astype(np.float64)
-    inside = np.zeros(n ** d, dtype=bool)
+    inside = np.zeros([n] * d, dtype=bool)
     for _ in range(nsph):
         c = rng.uniform(0, n, d)
         r = rng.uniform(0.03, 0.15) * n
-        dd = np.abs(pts - c)
-        dd = np.minimum(dd, n - dd)
-        inside |= (dd * dd).sum(1) < r * r
-    phase = inside.astype(np.int64)
+        # the sphere's periodic bounding box only (minimum-image distance per axis)
+        idx, dist2 = [], 0.0
+        for a in range(d):
+            lo, hi = int(np.floor(c[a] - r)), int(np.ceil(c[a] + r))
+            ii = np.arange(lo, hi + 1)
+            da = np.abs(ii - c[a])
+            da = np.minimum(da, n - da)
+            shape = [1] * d
+            shape[a] = ii.size
+            idx.append(np.mod(ii, n))
+            dist2 = dist2 + (da * da).reshape(shape)
+        inside[np.ix_(*idx)] |= dist2 < r * r
+    phase = inside.reshape(-1).astype(np.uint8)
     mats = []
     for k in range(2):
         E, nu = float(rng.uniform(1e9, 300e9)), float(rng.uniform(0.2, 0.4))
         if hep:
-            mats.append(('hep1', (E, nu, E * 1e-3, E * 5e-3)))
+            # the consistent tangent (mode 2), solved with newton_cg's line search
+            mats.append(('hep1', (E, nu, E * 1e-3, E * 5e-3, 2.0)))
         elif rng.random() < 0.5:
             mats.append(('le1', (E, nu)))
         else:
@@ -266,27 +279,47 @@ def _smooth235(n):
     return n == 1
 
 
-def run_stream(requests, rate_hz, server):
-    """Feed requests with Poisson arrivals (exponential gaps at rate_hz), wait for all."""
-    rng = np.random.default_rng(12345)
+def run_stream(requests, rate_hz, server, seed=12345):
+    """Feed requests open loop with Poisson arrivals (exponential gaps at rate_hz;
+    rate_hz <= 0 submits them all at once), wait for all.  A request the server
+    refuses at submission (larger than the HBM budget, invalid) counts as failed.
+    Throughput is over the wall time from the first submission to the last
+    completion."""
+    rng = np.random.default_rng(seed)
     server.start()
+    refused = {}
     t0 = time.perf_counter()
+    next_t = t0
     for req in requests:
-        server.submit(req)
         if rate_hz > 0:
-            time.sleep(float(rng.exponential(1.0 / rate_hz)))
+            now = time.perf_counter()
+            if next_t > now:
+                time.sleep(next_t - now)
+            next_t += float(rng.exponential(1.0 / rate_hz))
+        try:
+            server.submit(req)
+        except (L.CudaError, ValueError, RuntimeError) as e:
+            refused[req.rid] = str(e)[:60]
     server.close()
     server.join()
     wall = time.perf_counter() - t0
-    lat = np.array([r.latency for r in server.results.values()])
-    ok = sum(r.success for r in server.results.values())
+    res = server.results
+    lat = np.array([r.latency for r in res.values()]) if res else np.zeros(1)
+    ok = sum(r.success for r in res.values())
     laws = {req.rid: '+'.join(sorted({m[0] for m in req.materials})) for req in requests}
     failed = {}
-    for rid, r in server.results.items():
+    for rid, r in res.items():
         if not r.success:
             key = '%s: %s' % (laws.get(rid, '?'), r.message.split(' After ')[0][:60])
             failed[key] = failed.get(key, 0) + 1
-    return {'requests': len(requests), 'succeeded': int(ok), 'wall_s': wall, 'solves_per_s': len(requests) / wall,
-            'succeeded_per_s': int(ok) / wall, 'failed': failed,
+    for rid, msg in refused.items():
+        key = '%s: refused: %s' % (laws.get(rid, '?'), msg)
+        failed[key] = failed.get(key, 0) + 1
+    ok_lat = np.array([r.latency for r in res.values() if r.success]) if ok else np.zeros(1)
+    return {'requests': len(requests), 'succeeded': int(ok), 'refused': len(refused), 'wall_s': wall,
+            'offered_rate_hz': float(rate_hz) if rate_hz > 0 else None,
+            'solves_per_s': len(requests) / wall, 'succeeded_per_s': int(ok) / wall, 'failed': failed,
             'p50_ms': float(np.percentile(lat, 50) * 1e3), 'p99_ms': float(np.percentile(lat, 99) * 1e3),
+            'p50_ms_succeeded': float(np.percentile(ok_lat, 50) * 1e3),
+            'p99_ms_succeeded': float(np.percentile(ok_lat, 99) * 1e3),
             'peak_hbm_bytes': server.peak_in_use, 'batches': server.admitted_batches}

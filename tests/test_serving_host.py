@@ -4,6 +4,7 @@ completion, request validation, the config-5 request generator."""
 import numpy as np
 
 from muspectre_gb300 import serving
+from muspectre_gb300._lib import CudaError
 from muspectre_gb300.cell import Formulation
 
 
@@ -39,13 +40,18 @@ def test_admission_budget_and_batching():
     assert srv.peak_in_use <= srv.budget
 
 
-def test_oversized_request_admitted_alone():
-    srv = serving.Server(hbm_budget_bytes=1, lanes=0)
-    srv.submit(_req(0, 64))
-    g, used = srv._take()                          # an idle server admits it anyway
-    assert g == [0] and srv.in_use == used
-    g2, _ = srv._take()
-    assert g2 is None
+def test_oversized_request_refused():
+    """A request larger than the whole HBM budget is refused at submission (it would
+    overcommit the device even on an idle server); the server keeps serving."""
+    import pytest
+    fp = serving.estimate_bytes([64, 64], Formulation.finite_strain, False)
+    srv = serving.Server(hbm_budget_bytes=fp, lanes=0)
+    with pytest.raises(CudaError, match='budget'):
+        srv.submit(_req(0, 96))
+    srv.submit(_req(1, 64))
+    g, used = srv._take()
+    assert g == [1] and srv.in_use == used <= srv.budget
+    assert srv._take()[0] is None
 
 
 def test_batches_keep_shape_and_law_kind():
