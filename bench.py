@@ -70,6 +70,8 @@ def parse():
                     help='reference arm: complete oracle solves at any resolution (prints their counts)')
     ap.add_argument('--no-cpu', action='store_true')
     ap.add_argument('--no-extra', action='store_true', help='skip the other workloads (configs) of the metric')
+    ap.add_argument('--configs', default='readme,lognormal,voronoi,serving',
+                    help='the other workloads to run (comma list of readme, lognormal, voronoi, serving)')
     ap.add_argument('--only', default='all', choices=['all', 'mixed'],
                     help="'mixed': the mixed-precision solves only (for profiler launch lists)")
     return ap.parse_args()
@@ -353,7 +355,7 @@ def voronoi_config(mu, workloads, n=64):
     res = {}
     for prec in ('mixed', 'fp64'):
         c = cell_for('consistent')
-        s = mu.solvers.SolverCG(c, w['cg_tol'], w['maxiter'], precision=prec)
+        s = mu.solvers.SolverCG(c, w['cg_tol'], 1000, precision=prec)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         rs = mu.solvers.newton_cg(c, w['steps'], s, w['newton_tol'], w['equil_tol'], return_fields=False,
@@ -375,36 +377,48 @@ def voronoi_config(mu, workloads, n=64):
     return out
 
 
-def serving_config(mu, nreq=2000, lanes=4, max_batch=8, budget=96 << 30, sweep_n=200, sample=20):
+def serving_config(mu, nreq=2000, lanes=4, max_batch=8, budget=96 << 30, sweep_n=400, sample=20,
+                   deadline_s=150.0, sweep_deadline_s=40.0, sample_budget_s=60.0):
     """The serving stream: nreq seeded requests of mixed size, formulation, law and
     load path through the continuous-batching server (mixed precision).  Capacity: all
-    nreq submitted at once (open loop, far past saturation).  Rate sweep: sweep_n
-    requests at Poisson rates of 1/4, 1/2, 1 and 2 times that capacity, each on a
-    fresh server (succeeded solves/s, p50/p99 latency).  Accuracy: a seeded sample of
-    `sample` requests solved again alone in FP64 (the plain method, whose parity with
-    the oracle the tests pin); the homogenised-stress error of the served mixed result
-    against it."""
+    nreq submitted at once (open loop, far past saturation); requests still waiting
+    for admission deadline_s after the first submission are cancelled, so that the
+    leg stays within minutes (their count is reported; throughput counts succeeded
+    requests over the wall time).  Rate sweep: Poisson arrivals at 1/2, 1 and 2 times
+    that capacity for sweep_deadline_s each (from the first sweep_n requests), each on
+    a fresh server (succeeded solves/s, p50/p99 latency).  Accuracy: a seeded sample of up to `sample` served requests
+    solved again alone in FP64 (the plain method, whose parity with the oracle the
+    tests pin) within sample_budget_s; the homogenised-stress error of the served
+    mixed result against it."""
     from muspectre_gb300 import serving
     t0 = time.perf_counter()
     reqs = [serving.c5_request(i, 1000 + i) for i in range(nreq)]
     t_gen = time.perf_counter() - t0
     srv = serving.Server(budget, lanes=lanes, max_batch=max_batch, precision='mixed')
-    cap = serving.run_stream(reqs, rate_hz=0, server=srv)
+    cap = serving.run_stream(reqs, rate_hz=0, server=srv, deadline_s=deadline_s)
     mixed = dict(srv.results)
     del srv
+    progress('serving capacity run: %d succeeded, %d cancelled, %.1f s' % (cap['succeeded'], cap['cancelled'],
+                                                                           cap['wall_s']))
     capacity = cap['succeeded_per_s']
     sweep = []
-    for f in (0.25, 0.5, 1.0, 2.0):
+    for f in (0.5, 1.0, 2.0):
         s2 = serving.Server(budget, lanes=lanes, max_batch=max_batch, precision='mixed')
-        st = serving.run_stream(reqs[:sweep_n], rate_hz=f * capacity, server=s2, seed=77)
+        st = serving.run_stream(reqs[:sweep_n], rate_hz=f * capacity, server=s2, seed=77,
+                                deadline_s=sweep_deadline_s)
         sweep.append({'offered_hz': f * capacity, 'succeeded_per_s': st['succeeded_per_s'],
                       'p50_ms': st['p50_ms_succeeded'], 'p99_ms': st['p99_ms_succeeded'],
-                      'succeeded': st['succeeded'], 'requests': st['requests'], 'batches': st['batches']})
+                      'succeeded': st['succeeded'], 'cancelled': st['cancelled'], 'offered': st['offered'],
+                      'batches': st['batches']})
         del s2
+        progress('serving sweep at %.3g/s: %.3g succeeded/s' % (f * capacity, st['succeeded_per_s']))
     rng = np.random.default_rng(7)
-    picked = sorted(int(i) for i in rng.choice(nreq, size=sample, replace=False))
+    order = [int(i) for i in rng.permutation(nreq)]
     errs = {}
-    for i in picked:
+    t1 = time.perf_counter()
+    for i in order:
+        if len(errs) >= sample or time.perf_counter() - t1 > sample_budget_s:
+            break
         m = mixed.get(i)
         if m is None or not m.success:
             continue
@@ -412,23 +426,35 @@ def serving_config(mu, nreq=2000, lanes=4, max_batch=8, budget=96 << 30, sweep_n
         if r64.success:
             errs[i] = hom_err(m.stress, r64.stress)
     laws = [sorted({m[0] for m in r.materials}) for r in reqs]
-    cap.update({'arrivals': 'all %d submitted at once (open loop)' % nreq, 'lanes': lanes, 'max_batch': max_batch,
+    cap.update({'arrivals': 'all %d submitted at once (open loop), waiting ones cancelled after %g s'
+                % (nreq, deadline_s), 'lanes': lanes, 'max_batch': max_batch,
                 'hbm_budget_bytes': budget, 'request_generation_s': t_gen,
                 'elasto_plastic_requests': sum('hep1' in l for l in laws),
                 'rate_sweep': sweep,
-                'fp64_sample': {'requests': picked, 'compared': len(errs),
+                'fp64_sample': {'requests': sorted(errs), 'compared': len(errs),
                                 'stress_rel_err_max': max(errs.values()) if errs else None,
                                 'stress_rel_err_median': float(np.median(list(errs.values()))) if errs else None,
                                 'within_1e-6': sum(e <= 1e-6 for e in errs.values())}})
     return cap
 
 
-def extra_configs(mu, workloads, peak):
+def progress(msg):
+    print('[bench] ' + msg, file=sys.stderr, flush=True)
+
+
+def extra_configs(mu, workloads, peak, which):
     """The other workloads of the metric, each measured on this GPU (N=1 only)."""
-    return {'readme_51x51_fp64': readme_config(mu, workloads),
-            'lognormal256_le4_6rhs_mixed': lognormal_config(mu, workloads, peak),
-            'voronoi64_hep1_20steps': voronoi_config(mu, workloads),
-            'serving_stream_mixed': serving_config(mu)}
+    out = {}
+    for key, name, fn in (('readme', 'readme_51x51_fp64', lambda: readme_config(mu, workloads)),
+                          ('lognormal', 'lognormal256_le4_6rhs_mixed', lambda: lognormal_config(mu, workloads, peak)),
+                          ('voronoi', 'voronoi64_hep1_20steps', lambda: voronoi_config(mu, workloads)),
+                          ('serving', 'serving_stream_mixed', lambda: serving_config(mu))):
+        if key not in which:
+            continue
+        t0 = time.perf_counter()
+        out[name] = fn()
+        progress('%s: %.1f s' % (name, time.perf_counter() - t0))
+    return out
 
 
 def run_reference(args, rank, world):
@@ -579,6 +605,7 @@ def main():
                               'iteration_us': round(tot * 1e3, 1)}), flush=True)
         return
 
+    progress('mixed: %.2f solves/s' % value)
     # ---------------- FP64 method on the same input
     fp64_lat = []
     for i in range(1 + args.fp64_steps):
@@ -608,6 +635,7 @@ def main():
                      'frac_of_fp64_fma': (fl / (ms * 1e-3) / 1e12) / fp64_peak if ms > 0 else None,
                      'gbs': algorithmic_bytes(name, npx, nk, d2, 8, 8 * 18) / (ms * 1e-3) / 1e9 if ms > 0 else None}
 
+    progress('fp64: %.3f solves/s' % fp64_sps)
     # ---------------- end to end through the public API from host buffers
     e2e_t = []
     h2d = npx  # the material index byte per pixel (the Lame planes are filled on the device from it)
@@ -648,9 +676,11 @@ def main():
         'e2e': {'value': e2e_v, 'unit': 'solves/s', 'h2d_bytes_per_step': h2d, 'd2h_bytes_per_step': d2h},
     }
     if rank == 0 and world == 1 and not args.no_extra:
-        line['configs'] = extra_configs(mu, workloads, peak)
+        line['configs'] = extra_configs(mu, workloads, peak, args.configs.split(','))
     if rank == 0 and not args.no_cpu:
+        t0 = time.perf_counter()
         cb = cpu_baseline(w, args.cpu_cg_iters)
+        progress('cpu baseline: %.1f s' % (time.perf_counter() - t0))
         line['cpu_baseline'] = {'value': cb['solves_per_s'], 'unit': 'solves/s', 'cores': cb['cores'], 'kind': 'port',
                                 'sample': cb['sample'], 'pxit_per_s': cb['pxit_per_s']}
     if pg:

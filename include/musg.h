@@ -192,8 +192,9 @@ int musg_solver_set_inner_tol(musg_solver *solver, double inner_tol);
 /* newton_cg with a backtracking line search (no counterpart in the reference; off by
  * default): every Newton increment dF is applied as F0 + lam dF with lam = 1, 1/2, ...
  * until the norm of the projected residual G(-P) falls below (1 - 1e-4 lam) of the
- * current one, or lam = 1/1024; the convergence test still measures |dF|.  It lets the
- * consistent elasto-plastic tangent (HEP1 mode 2) converge on heterogeneous cells. */
+ * current one, or lam = 1/1024; the convergence test still measures |dF|, and a load
+ * step takes at most min(maxiter, 100) Newton iterations.  It lets the consistent
+ * elasto-plastic tangent (HEP1 mode 2) converge on heterogeneous cells. */
 int musg_solver_set_line_search(musg_solver *solver, int enable);
 /* SolverBase::get_counter / reset_counter / has_converged (solver_base.hh:62-109) */
 int musg_solver_get_counter(musg_solver *solver, unsigned *counter);
@@ -220,14 +221,18 @@ int musg_de_geus(musg_cell *cell, const double *load_steps, int nb_steps,
                  double *stresses);
 
 /* -------------------------------------------------------------- batches
- * Many same-shape cells (RVEs, or right-hand sides on copies of one microstructure)
- * solved together: newton_cg's Newton steps run in lockstep per cell and every CG
- * iteration is one launch per pass for all cells (replayed from one CUDA graph).
- * No counterpart in the reference, which solves one cell at a time; each cell's
- * results equal those of musg_newton_cg on it alone.  load_steps: nb_cells x
- * nb_steps D*D column-major matrices; infos: nb_cells x nb_steps records; stresses
- * (may be NULL): nb_cells x nb_steps x nb_dof.  A cell whose CG fails is reported
- * (success 0, the ConvergenceError message) and leaves the batch. */
+ * Many cells (RVEs, or right-hand sides on copies of one microstructure) solved
+ * together: newton_cg's Newton steps run in lockstep per cell and every CG iteration
+ * is one launch per pass for all cells (replayed from one CUDA graph).  No
+ * counterpart in the reference, which solves one cell at a time.  Cells of one grid
+ * run the solo solve's kernels (results equal those of musg_newton_cg on each cell
+ * alone, bit for bit); cells of different grids (same dimension, formulation and
+ * material-law kind) run grouped launches of the generic pass kernels, each cell
+ * owning a range of blocks and its own plans (results equal to the solo ones within
+ * rounding).  load_steps: nb_cells x nb_steps D*D column-major matrices; infos:
+ * nb_cells x nb_steps records; stresses (may be NULL): for each cell in turn,
+ * nb_steps x its nb_dof.  A cell whose CG fails is reported (success 0, the
+ * ConvergenceError message) and leaves the batch. */
 int musg_batch_create(musg_cell **cells, int nb_cells, double tol, unsigned maxiter,
                       int precision, musg_batch **out);
 int musg_batch_destroy(musg_batch *batch);
@@ -240,13 +245,15 @@ int musg_batch_newton_cg(musg_batch *batch, const double *load_steps, int nb_ste
  * A continuous-batching request server (no counterpart in the reference, which
  * solves one cell per process).  Requests are admitted while their estimated device
  * footprint (musg_request_bytes) fits the HBM budget next to the requests already
- * running; waiting requests of the same shape (grid, formulation, material-law
- * kind, number of load steps) are taken together and solved as one batch
- * (musg_batch_*).  Each lane is a host thread with its own CUDA stream, so admitted
+ * running; waiting requests of the same kind (dimension, formulation, material-law
+ * kind, number of load steps; grids within a factor 8 in pixels) are taken together
+ * and solved as one batch (musg_batch_*: one launch per CG pass, grouped over
+ * different grids).  Each lane is a host thread with its own CUDA stream, so admitted
  * work overlaps on the device; a request's fields and plastic state stay on the
- * device for all its load steps and return to the budget when it completes.  Every
- * request gets the same kernels in the same order alone or in a batch, so its result
- * does not depend on what else runs. */
+ * device for all its load steps and return to the budget when it completes.  A
+ * request batched with requests of its own grid gets the kernels of its solo solve in
+ * the same order (the same result bit for bit); batched with other grids it runs the
+ * generic pass kernels (the same result within rounding). */
 typedef struct musg_server musg_server;
 
 /* one request; the server copies everything at submission */
@@ -281,6 +288,7 @@ typedef struct musg_server_result {
 typedef struct musg_server_stats {
   long long submitted, completed, batches;
   unsigned long long budget, in_use, peak_in_use;
+  long long queued;  /* submitted, not yet admitted */
 } musg_server_stats;
 
 /* device bytes a request holds while it runs (fields, spectra, tangent data, CG
@@ -293,6 +301,10 @@ int musg_server_create(unsigned long long hbm_budget, int lanes, int max_batch, 
 int musg_server_submit(musg_server *srv, const musg_request *req, long long *id);
 /* no more submissions; lanes finish the queue and exit */
 int musg_server_close(musg_server *srv);
+/* drops the requests still waiting for admission: each completes at once, unsolved,
+ * with the message "cancelled before admission" (a deadline on a stream); running
+ * groups finish.  *cancelled (may be NULL) receives their number. */
+int musg_server_cancel_waiting(musg_server *srv, long long *cancelled);
 /* result of request id, waiting at most timeout_s seconds (MUSG_ERR_RUNTIME when it
  * is not done by then); a result can be fetched once */
 int musg_server_wait(musg_server *srv, long long id, double timeout_s, musg_server_result *out);
@@ -300,7 +312,7 @@ int musg_server_get_stats(musg_server *srv, musg_server_stats *out);
 /* closes the server and joins its lanes */
 int musg_server_destroy(musg_server *srv);
 /* the admission step of a lane: the oldest waiting request that fits the budget next
- * to the running ones and the waiting requests of its shape that fit too, at most cap
+ * to the running ones and the waiting requests of its kind that fit too, at most cap
  * (a request with the consistent elasto-plastic tangent, solved with the line search,
  * is taken alone); their ids, count and bytes (now counted as in use).  A request
  * larger than the whole budget is refused by musg_server_submit (MUSG_ERR_MEMORY). */

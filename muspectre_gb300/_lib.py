@@ -60,7 +60,8 @@ class ServerResult(C.Structure):
 
 class ServerStats(C.Structure):
     _fields_ = [('submitted', C.c_longlong), ('completed', C.c_longlong), ('batches', C.c_longlong),
-                ('budget', C.c_ulonglong), ('in_use', C.c_ulonglong), ('peak_in_use', C.c_ulonglong)]
+                ('budget', C.c_ulonglong), ('in_use', C.c_ulonglong), ('peak_in_use', C.c_ulonglong),
+                ('queued', C.c_longlong)]
 
 
 _P = C.c_void_p
@@ -130,6 +131,7 @@ _SIGNATURES = {
                                      C.POINTER(_P)]),
     'musg_server_submit': (C.c_int, [_P, C.POINTER(Request), _LL]),
     'musg_server_close': (C.c_int, [_P]),
+    'musg_server_cancel_waiting': (C.c_int, [_P, _LL]),
     'musg_server_wait': (C.c_int, [_P, C.c_longlong, C.c_double, C.POINTER(ServerResult)]),
     'musg_server_get_stats': (C.c_int, [_P, C.POINTER(ServerStats)]),
     'musg_server_destroy': (C.c_int, [_P]),

@@ -1,11 +1,14 @@
-"""Batched Newton-CG over many same-shape cells (RVEs or load cases).
+"""Batched Newton-CG over many cells (RVEs or load cases).
 
 ``BatchSolver(cells, tol, maxiter, precision)`` solves every cell with the method of
 ``solvers.newton_cg``; the Newton steps of the cells run in lockstep and every CG
-iteration is a single launch per spectral pass for all cells (problem index =
-blockIdx.y), replayed from one CUDA graph.  Each cell's results are those of a
-solo ``newton_cg`` call on it.  Cells of different shape go into separate batches
-(shape buckets).
+iteration is a single launch per spectral pass for all cells, replayed from one CUDA
+graph.  Cells of one grid run the solo kernels with problem index = blockIdx.y, and
+each cell's results are those of a solo ``newton_cg`` call on it, bit for bit.  Cells
+of different grids (same dimension, formulation and material-law kind) run grouped
+launches: each cell owns a range of the grid's blocks and its own FFT plans and
+sizes (the generic pass kernels), with results equal to the solo ones within
+rounding.
 """
 from __future__ import annotations
 
@@ -62,17 +65,19 @@ class BatchSolver:
         ns = a.shape[1]
         flat = np.ascontiguousarray(a.transpose(0, 1, 3, 2)).reshape(-1)  # column-major matrices
         infos = (L.ResultInfo * (B * ns))()
-        nd = self.cells[0].nb_dof
-        stresses = np.empty((B, ns, nd)) if return_stress else None
+        sizes = [c.nb_dof for c in self.cells]
+        offs = np.concatenate([[0], np.cumsum([ns * n for n in sizes])]).astype(np.int64)
+        flat_s = np.empty(int(offs[-1])) if return_stress else None  # cell after cell, ns x nb_dof each
         L.check(L.lib().musg_batch_newton_cg(self._h, L.dptr(flat), ns, float(newton_tol), float(equil_tol), infos,
-                                             L.dptr(stresses)))
+                                             L.dptr(flat_s)))
         out = []
         for b in range(B):
             rs = []
+            st_b = flat_s[offs[b]:offs[b + 1]].reshape(ns, sizes[b]) if return_stress else None
             for k in range(ns):
                 i = infos[b * ns + k]
                 rs.append(OptimizeResult(np.empty((0, 1)),
-                                         stresses[b, k].reshape(-1, 1) if return_stress else np.empty((0, 1)),
+                                         st_b[k].reshape(-1, 1) if return_stress else np.empty((0, 1)),
                                          bool(i.success), int(i.status), i.message.decode(), int(i.nb_it),
                                          int(i.nb_fev), np.array(i.hom_stress[:d * d]).reshape(d, d).T))
             self.cells[b]._has_tangent = True

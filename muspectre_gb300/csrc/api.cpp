@@ -746,8 +746,14 @@ struct musg_batch {
   cudaGraphExec_t exec = nullptr;
   unsigned long long graph_nodes = 0;
   int chunk = 16;
+  // cells of different grids (the same dimension, formulation and tangent kind): one
+  // grouped launch per pass over all of them (generic pass kernels)
+  bool uniform = true;
+  GroupedOp *gop = nullptr;
+  long long nmax = 0;  // the largest cell's vector length
 
   ~musg_batch() {
+    if (gop) grouped_op_destroy(gop);
     if (exec) cudaGraphExecDestroy(exec);
     if (hst) cudaFreeHost(hst);
     if (stream) cudaStreamDestroy(stream);
@@ -777,6 +783,24 @@ struct musg_batch {
       tv[b].p = sv.p.as<R>();
       tv[b].Ap = sv.Ap.as<R>();
       tv[b].partial = c.partial.as<double>();
+      tv[b].n = c.nb_dof();
+      tv[b].nparts = 0;
+      nmax = std::max(nmax, c.nb_dof());
+    }
+    if (!uniform) {
+      std::vector<GroupProblem> probs(B());
+      for (int b = 0; b < B(); ++b) {
+        probs[b].sp = &cells[b]->sp;
+        probs[b].st = state(b);
+        probs[b].r = tp[b].r;
+        probs[b].x = tp[b].x;
+        probs[b].p = tp[b].p;
+        probs[b].Ap = tp[b].Ap;
+        probs[b].partial = tp[b].partial;
+        memcpy(probs[b].td, tp[b].td, sizeof(probs[b].td));
+      }
+      gop = grouped_op_create<R>(probs, cells[0]->tk<R>());
+      for (int b = 0; b < B(); ++b) tv[b].nparts = grouped_op_fwd_partials(gop, b);
     }
     tab_p.alloc(tp.size() * sizeof(ProblemPtrsHost));
     tab_v.alloc(tv.size() * sizeof(BatchVec<R>));
@@ -786,10 +810,12 @@ struct musg_batch {
 
   template <typename R> void iteration(cudaStream_t s) {
     musg_cell &c0 = *cells[0];
-    const long long n = c0.nb_dof();
-    cg_operator_batch<R>(c0.sp, c0.tk<R>(), (const ProblemPtrs<R> *)tab_p.p, tab_v.as<BatchVec<R>>(), B(),
-                         s);  // and alpha (FP32: the whole iteration)
-    if (sizeof(R) == 8) cg_update_batch<R>(tab_v.as<BatchVec<R>>(), n, B(), s);  // and beta
+    if (uniform)
+      cg_operator_batch<R>(c0.sp, c0.tk<R>(), (const ProblemPtrs<R> *)tab_p.p, tab_v.as<BatchVec<R>>(), B(),
+                           s);  // and alpha (FP32: the whole iteration)
+    else
+      grouped_op_run<R>(gop, tab_v.as<BatchVec<R>>(), nmax, B(), s);
+    if (sizeof(R) == 8) cg_update_batch<R>(tab_v.as<BatchVec<R>>(), nmax, B(), s);  // and beta
   }
 
   template <typename R> void build_graph() {
@@ -813,14 +839,13 @@ struct musg_batch {
 
   // one batched SolverCG::solve over the cells whose `solve` flag is set
   template <typename R> void solve(const std::vector<char> &solve_it, std::vector<std::string> &errors) {
-    const long long n = cells[0]->nb_dof();
     const double t = (precision == MUSG_PRECISION_MIXED) ? std::max(tol, inner_tol) : tol;
     for (int b = 0; b < B(); ++b) {
       musg_cell &c = *cells[b];
       double *part = c.partial.as<double>();
       if (solve_it[b]) {
-        cg_init<R>(state(b), c.rhs.as<double>(), solvers[b]->r.as<R>(), solvers[b]->x.as<R>(), n, t, (int)maxiter,
-                   part, part + 4096, stream);
+        cg_init<R>(state(b), c.rhs.as<double>(), solvers[b]->r.as<R>(), solvers[b]->x.as<R>(), c.nb_dof(), t,
+                   (int)maxiter, part, part + 4096, stream);
       } else {
         MUSG_CUDA(cudaMemsetAsync(&state(b)->active, 0, sizeof(int), stream));
       }
@@ -873,6 +898,8 @@ struct musg_projection {
 
 // ---------------------------------------------------------------------- newton_cg
 namespace {
+
+constexpr unsigned kLineSearchNewtonMax = 100;
 
 void check_symmetry_or_throw(const double *m, int dim) {
   // solver_common.cc:39-43 with rel_tol = 1e-8
@@ -934,7 +961,11 @@ void newton_cg_impl(musg_cell *cell, const double *steps, int nsteps, musg_solve
     };
     unsigned newt_iter = 0;
     bool evaluated = false;  // a line-search trial left P and rhs at the current F
-    for (; newt_iter < solver->maxiter && !has_converged; ++newt_iter) {
+    // the reference bounds the Newton loop by the CG solver's maxiter
+    // (solvers.cc:150); with the line search, whose damped steps can creep, at most
+    // kLineSearchNewtonMax iterations per load step
+    const unsigned newton_max = solver->line_search ? std::min(solver->maxiter, kLineSearchNewtonMax) : solver->maxiter;
+    for (; newt_iter < newton_max && !has_converged; ++newt_iter) {
       const bool first_geus = geus && newt_iter == 0;
       if (evaluated) {
         evaluated = false;
@@ -1027,7 +1058,6 @@ void batch_newton_impl(musg_batch *batch, const double *steps, int nsteps, doubl
   const int B = bt.B();
   musg_cell &c0 = *bt.cells[0];
   const int dim = c0.dim, D2 = c0.D2;
-  const long long n = c0.nb_dof();
   cudaStream_t s = bt.stream;
   std::vector<cudaStream_t> saved(B);
   for (int b = 0; b < B; ++b) {
@@ -1047,7 +1077,7 @@ void batch_newton_impl(musg_batch *batch, const double *steps, int nsteps, doubl
   else
     for (int k = 0; k < B * nsteps; ++k) check_symmetry_or_throw(steps + (size_t)k * D2, dim);
   for (int b = 0; b < B; ++b)
-    fill_uniform(bt.cells[b]->F.as<double>(), bt.cells[b]->put_matrix(I.data(), 0), D2, c0.npx, s);
+    fill_uniform(bt.cells[b]->F.as<double>(), bt.cells[b]->put_matrix(I.data(), 0), D2, bt.cells[b]->npx, s);
   std::vector<std::vector<double>> previous(B, std::vector<double>(D2, 0.0));
   std::vector<char> failed(B, 0);
   std::vector<std::string> errmsg(B);
@@ -1086,7 +1116,7 @@ void batch_newton_impl(musg_batch *batch, const double *steps, int nsteps, doubl
         musg_cell &c = *bt.cells[b];
         c.evaluate(false);
         spectral_project<double>(c.sp, c.P.as<double>(), c.rhs.as<double>(), -1.0, s);
-        dot_device<double, double>(c.rhs.as<double>(), c.rhs.as<double>(), n, c.partial.as<double>(),
+        dot_device<double, double>(c.rhs.as<double>(), c.rhs.as<double>(), c.nb_dof(), c.partial.as<double>(),
                                    c.scal.as<double>() + 32, s);
         MUSG_CUDA(cudaMemcpyAsync(c.hscal + 32, c.scal.as<double>() + 32, sizeof(double), cudaMemcpyDeviceToHost, s));
       }
@@ -1116,9 +1146,11 @@ void batch_newton_impl(musg_batch *batch, const double *steps, int nsteps, doubl
         musg_cell &c = *bt.cells[b];
         double *dscal = c.scal.as<double>();
         if (bt.precision == MUSG_PRECISION_MIXED)
-          newton_update<float>(c.F.as<double>(), bt.solvers[b]->x.as<float>(), n, c.partial.as<double>(), dscal + 34, s);
+          newton_update<float>(c.F.as<double>(), bt.solvers[b]->x.as<float>(), c.nb_dof(), c.partial.as<double>(),
+                               dscal + 34, s);
         else
-          newton_update<double>(c.F.as<double>(), bt.solvers[b]->x.as<double>(), n, c.partial.as<double>(), dscal + 34,
+          newton_update<double>(c.F.as<double>(), bt.solvers[b]->x.as<double>(), c.nb_dof(), c.partial.as<double>(),
+                                dscal + 34,
                                 s);
         MUSG_CUDA(cudaMemcpyAsync(c.hscal + 34, dscal + 34, 2 * sizeof(double), cudaMemcpyDeviceToHost, s));
       }
@@ -1145,7 +1177,12 @@ void batch_newton_impl(musg_batch *batch, const double *steps, int nsteps, doubl
       strncpy(ri.message, failed[b] ? errmsg[b].c_str() : message[b].c_str(), sizeof(ri.message) - 1);
       if (!failed[b]) c.homogenised(ri.hom_stress);
       else std::fill(ri.hom_stress, ri.hom_stress + 9, std::nan(""));
-      if (stresses && !failed[b]) c.download_field(c.P.as<double>(), stresses + ((size_t)b * nsteps + step) * n);
+      if (stresses && !failed[b]) {
+        // cells one after another, each nb_steps x its nb_dof (the uniform layout when all match)
+        size_t off = 0;
+        for (int k = 0; k < b; ++k) off += (size_t)nsteps * bt.cells[k]->nb_dof();
+        c.download_field(c.P.as<double>(), stresses + off + (size_t)step * c.nb_dof());
+      }
       if (!failed[b]) c.save_history();
     }
   }
@@ -1725,9 +1762,10 @@ int musg_batch_create(musg_cell **cells, int nb_cells, double tol, unsigned maxi
       musg_cell &c = *cells[b];
       require(cells[b] != nullptr, MUSG_ERR_ARGUMENT, "null cell");
       if (!c.initialised) c.initialise();
-      require(c.dim == c0.dim && c.form == c0.form && c.res[0] == c0.res[0] && c.res[1] == c0.res[1] &&
-                  c.res[2] == c0.res[2] && c.flags == c0.flags && c.tkind == c0.tkind && c.tkind32 == c0.tkind32,
-              MUSG_ERR_ARGUMENT, "cells of a batch need the same grid, formulation and material-law kind");
+      require(c.dim == c0.dim && c.form == c0.form && c.flags == c0.flags && c.tkind == c0.tkind &&
+                  c.tkind32 == c0.tkind32,
+              MUSG_ERR_ARGUMENT, "cells of a batch need the same dimension, formulation and material-law kind");
+      if (c.res[0] != c0.res[0] || c.res[1] != c0.res[1] || c.res[2] != c0.res[2]) bt->uniform = false;
       for (int k = 0; k < b; ++k) require(cells[k] != cells[b], MUSG_ERR_ARGUMENT, "a cell appears twice in a batch");
       auto sv = std::make_unique<musg_solver>();
       sv->create(&c, tol, maxiter, 0, precision);

@@ -181,11 +181,12 @@ template <typename R> __device__ __forceinline__ void update_x_body(R alpha, R *
 }
 
 // alpha = r.r / p.(K:p) of problem blockIdx.x (a table of states and partial arrays,
-// or one state and array)
+// or one state and array; nparts < 0: each problem's own count from the table)
 __global__ void k_cg_alpha(CGState *st, const double *partial, const BatchVec<float> *tab, int nparts) {
   dep_wait();
   CGState *s = tab ? tab[blockIdx.x].st : st;
   const double *part = tab ? tab[blockIdx.x].partial : partial;
+  if (nparts < 0) nparts = tab[blockIdx.x].nparts;
   if (!s->active) return;
   const double pAp = sum_partials_fresh(part, nparts);
   if (threadIdx.x == 0) {
@@ -215,7 +216,8 @@ template <typename R> __global__ void k_cg_update_x_b(const BatchVec<R> *tab, lo
   dep_wait();
   const BatchVec<R> q = tab[blockIdx.y];
   if (!q.st->active) return;
-  update_x_body<R>(R(q.st->alpha), q.x, q.p, n);
+  update_x_body<R>(R(q.st->alpha), q.x, q.p, q.n);  // the problem's own length (n: the largest)
+  (void)n;
 }
 
 template <typename R> void cg_update_x_batch(const BatchVec<R> *tab, long long n, int nparts, int B, cudaStream_t s) {
@@ -236,7 +238,8 @@ __global__ void k_cg_update_b(const BatchVec<R> *tab, long long n) {
   dep_wait();
   const BatchVec<R> q = tab[blockIdx.y];
   if (!q.st->active) return;
-  const double bs = cg_update_body<R>(R(q.st->alpha), q.x, q.r, q.p, q.Ap, n);
+  const double bs = cg_update_body<R>(R(q.st->alpha), q.x, q.r, q.p, q.Ap, q.n);  // n: the largest
+  (void)n;
   if (threadIdx.x == 0) q.partial[blockIdx.x] = bs;
   if (cg_last_block(q.st)) cg_beta_step(q.st, q.partial, gridDim.x);
 }

@@ -242,6 +242,26 @@ template <typename R> struct BatchVec;
 template <typename R>
 int cg_operator_batch(Spectral &sp, int tkind, const ProblemPtrs<R> *tab, const BatchVec<R> *xtab, int B,
                       cudaStream_t s);
+// Grouped CG operator over problems of different grids (the same dimension,
+// projection and tangent kind): one launch per pass for all of them, problem b
+// owning a contiguous range of the one-dimensional grid (generic pass kernels, whose
+// plans and sizes are runtime values).  The per-problem arguments live in device
+// tables built once; run launches one CG iteration's passes (FP32: with cg_alpha /
+// cg_update_x over xtab between the forward and the middle passes).
+struct GroupProblem {
+  Spectral *sp;
+  const CGState *st;
+  void *r, *x, *p, *Ap;
+  double *partial;
+  unsigned char td[sizeof(TangentData<double>)];
+};
+struct GroupedOp;
+template <typename R> GroupedOp *grouped_op_create(const std::vector<GroupProblem> &probs, int tkind);
+void grouped_op_destroy(GroupedOp *op);
+// partial sums the grouped forward pass writes for problem b (its blocks x warps)
+int grouped_op_fwd_partials(const GroupedOp *op, int b);
+template <typename R>
+void grouped_op_run(GroupedOp *op, const BatchVec<R> *xtab, long long nmax, int B, cudaStream_t s);
 // Times candidate launch shapes of each pass on this grid (CUDA events) and keeps
 // the fastest (FFT_PlanFlags::measure / patient); fp32 selects the FP32 passes.
 template <typename R> void spectral_autotune(Spectral &sp, cudaStream_t s, int effort);
@@ -267,6 +287,8 @@ template <typename R> struct BatchVec {
   const R *p;
   const R *Ap;
   double *partial;
+  long long n;  // entries of the problem's vectors
+  int nparts;   // the forward pass's partial sums of the problem (grouped launches)
 };
 template <typename R>
 void cg_update_batch(const BatchVec<R> *tab, long long n, int B, cudaStream_t s);

@@ -1,12 +1,14 @@
 // Continuous-batching request server (musg_server_*), built on the library's own
 // C ABI: every request becomes a cell (musg_cell_*), solved alone by musg_newton_cg
-// or with same-shape requests by musg_batch_newton_cg.
+// or with requests of its kind by musg_batch_newton_cg.
 //
 // Admission: a lane takes the oldest waiting request whose device footprint fits the
 // HBM budget next to the requests already running (a request larger than the whole
-// budget is refused at submission), plus the waiting requests of the same shape that
-// fit too, up to max_batch (requests with the consistent elasto-plastic tangent run
-// alone, with newton_cg's line search).  Lanes are host threads,
+// budget is refused at submission), plus the waiting requests of the same kind
+// (dimension, formulation, law kind, load steps; grids within a factor 8 in pixels)
+// that fit too, up to max_batch; a batch of several grids runs grouped launches
+// (requests with the consistent elasto-plastic tangent run alone, with newton_cg's
+// line search).  Lanes are host threads,
 // each with its own non-blocking CUDA stream, so admitted groups overlap on the
 // device.  A group's memory returns to the budget when it completes.  Latency is
 // measured from submission to completion on the host's steady clock.
@@ -136,9 +138,10 @@ std::shared_ptr<Req> copy_request(const musg_request &src, int precision) {
   int res[3] = {1, 1, 1};
   for (int d = 0; d < src.dim; ++d) res[d] = src.resolutions[d];
   q->bytes = footprint(src.dim, res, src.formulation, q->has_hep, q->has_full, precision);
-  // same shape = same grid, formulation, flags, number of steps and tangent kind
-  q->key = std::make_tuple(src.dim, res[0], res[1], res[2], src.formulation, src.flags, src.nb_steps,
-                           (int)q->has_hep, (int)q->any_le, (int)q->has_le2, (int)q->has_full);
+  // batchable together = same dimension, formulation, flags, number of steps and
+  // tangent kind (grids may differ: a batch of several grids runs grouped launches)
+  q->key = std::make_tuple(src.dim, 0, 0, 0, src.formulation, src.flags, src.nb_steps, (int)q->has_hep,
+                           (int)q->any_le, (int)q->has_le2, (int)q->has_full);
   return q;
 }
 
@@ -208,7 +211,10 @@ struct musg_server {
       // requests solved with the line search (consistent elasto-plastic tangent) run alone
       for (size_t k = i + 1; k < queue.size() && (int)group.size() < max_batch && !q->has_full; ++k) {
         const auto &o = queue[k];
-        if (o->key == q->key && in_use + used + o->bytes <= budget) {
+        // grids within a factor 8 in pixels of the first: the batch's Newton steps run
+        // in lockstep, so a much larger cell would hold the smaller ones back
+        const bool close = o->npx <= 8 * q->npx && q->npx <= 8 * o->npx;
+        if (o->key == q->key && close && in_use + used + o->bytes <= budget) {
           group.push_back(o);
           used += o->bytes;
         }
@@ -410,6 +416,30 @@ int musg_server_close(musg_server *srv) {
   });
 }
 
+int musg_server_cancel_waiting(musg_server *srv, long long *cancelled) {
+  return guarded([&] {
+    need(srv != nullptr, MUSG_ERR_ARGUMENT, "null server");
+    long long n = 0;
+    {
+      std::lock_guard<std::mutex> lk(srv->mu);
+      const Clock::time_point t1 = Clock::now();
+      for (const auto &q : srv->queue) {
+        musg_server_result res;
+        std::memset(&res, 0, sizeof(res));
+        res.id = q->id;
+        res.latency_s = std::chrono::duration<double>(t1 - q->t0).count();
+        set_message(res, "cancelled before admission");
+        srv->done[q->id] = res;
+        ++n;
+      }
+      srv->queue.clear();
+      srv->completed += n;
+    }
+    srv->cv.notify_all();
+    if (cancelled) *cancelled = n;
+  });
+}
+
 int musg_server_wait(musg_server *srv, long long id, double timeout_s, musg_server_result *out) {
   return guarded([&] {
     need(srv && out, MUSG_ERR_ARGUMENT, "null argument");
@@ -436,6 +466,7 @@ int musg_server_get_stats(musg_server *srv, musg_server_stats *out) {
     out->budget = srv->budget;
     out->in_use = srv->in_use;
     out->peak_in_use = srv->peak;
+    out->queued = (long long)srv->queue.size();
   });
 }
 

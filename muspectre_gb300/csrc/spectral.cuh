@@ -115,16 +115,30 @@ __device__ __forceinline__ int warps_per_block() { return (blockDim.x * blockDim
 __device__ __forceinline__ int lin_tid() { return threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z); }
 __device__ __forceinline__ int lin_nth() { return blockDim.x * blockDim.y * blockDim.z; }
 
-// call by the whole block after thread 0 wrote this block's partial sum
-__device__ __forceinline__ bool cg_last_block(CGState *st) {
+// call by the whole block after thread 0 wrote this block's partial sum; nblk = the
+// problem's blocks (gridDim.x, or a problem's share of a grouped launch)
+__device__ __forceinline__ bool cg_last_block(CGState *st, int nblk) {
   __shared__ int last;
   __syncthreads();
   if (lin_tid() == 0) {
     __threadfence();
-    last = atomicAdd(&st->ticket, 1) == (int)gridDim.x - 1;
+    last = atomicAdd(&st->ticket, 1) == nblk - 1;
   }
   __syncthreads();
   return last != 0;
+}
+__device__ __forceinline__ bool cg_last_block(CGState *st) { return cg_last_block(st, (int)gridDim.x); }
+
+// Grouped launches: problems of different grids in one launch, the blocks of problem b
+// being [blk0[b], blk0[b+1]) of a one-dimensional grid; b by binary search
+__device__ __forceinline__ int group_problem(const int *blk0, int B) {
+  int lo = 0, hi = B;
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (blk0[mid] <= (int)blockIdx.x) lo = mid;
+    else hi = mid;
+  }
+  return lo;
 }
 
 __device__ __forceinline__ double sum_partials_fresh(const double *partial, int n) {
@@ -432,13 +446,10 @@ template <typename R> struct LastArgs {
 };
 
 // forward: real rows -> half spectra.  D is the tensor dimension for the tangent
-// prologues (0 for PRO_PLAIN).
+// prologues (0 for PRO_PLAIN).  bid: this block among the problem's blocks.
 template <typename R, int PRO, int D, int TK>
-__global__ void __launch_bounds__(kPassThreads) k_last_fwd(const LastArgs<R> a0) {
-  dep_wait();
+__device__ __forceinline__ void last_fwd_body(const LastArgs<R> &a, long long bid) {
   using T = typename V2<R>::T;
-  LastArgs<R> a = a0;
-  a.bind();
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T *buf = reinterpret_cast<T *>(smem_raw);
   constexpr bool kCG = PRO == PRO_CG || PRO == PRO_CGF;
@@ -447,7 +458,7 @@ __global__ void __launch_bounds__(kPassThreads) k_last_fwd(const LastArgs<R> a0)
   Acc<R> pkp;  // PRO_CGF: partial sum of p.(K:p)
   const int P = nc * G2;
   T *buf2 = buf + (size_t)P * a.ap.m;
-  const long long row0 = (long long)blockIdx.x * G;
+  const long long row0 = bid * G;
   R *bufr = reinterpret_cast<R *>(buf);
   const FDiv fGL(G * L), fL(L);
   if constexpr (PRO == PRO_PLAIN) {
@@ -539,24 +550,37 @@ __global__ void __launch_bounds__(kPassThreads) k_last_fwd(const LastArgs<R> a0)
     else o = T{R(0.5) * (z.y + zn.y), R(-0.5) * (z.x - zn.x)};
     a.spec[(long long)c * a.nk + row * H + k] = o;
   }
-  if constexpr (PRO == PRO_CGF) warp_partial(pkp.value(), a.partial + (size_t)blockIdx.x * warps_per_block());
+  if constexpr (PRO == PRO_CGF) warp_partial(pkp.value(), a.partial + (size_t)bid * warps_per_block());
+}
+
+template <typename R, int PRO, int D, int TK>
+__global__ void __launch_bounds__(kPassThreads) k_last_fwd(const LastArgs<R> a0) {
+  dep_wait();
+  LastArgs<R> a = a0;
+  a.bind();
+  last_fwd_body<R, PRO, D, TK>(a, blockIdx.x);
+}
+
+template <typename R, int PRO, int D, int TK>
+__global__ void __launch_bounds__(kPassThreads) k_last_fwd_g(const LastArgs<R> *tab, const int *blk0, int B) {
+  dep_wait();
+  const int b = group_problem(blk0, B);
+  const LastArgs<R> a = tab[b];
+  last_fwd_body<R, PRO, D, TK>(a, blockIdx.x - blk0[b]);
 }
 
 // inverse: half spectra -> real rows.  PLAIN writes out = scale*x; CG writes Ap
 // and the block sums of p.Ap.
 template <typename R, int EPI, int D>
-__global__ void __launch_bounds__(kPassThreads) k_last_inv(const LastArgs<R> a0) {
-  dep_wait();
+__device__ __forceinline__ void last_inv_body(const LastArgs<R> &a, long long bid, int nblk) {
   using T = typename V2<R>::T;
-  LastArgs<R> a = a0;
-  a.bind();
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T *buf = reinterpret_cast<T *>(smem_raw);
   if (EPI != EPI_PLAIN && !a.st->active) return;
   const int L = a.L, G = a.G, nc = a.ncomp, G2 = G >> 1, H = a.H;
   const int P = nc * G2;
   T *buf2 = buf + (size_t)P * a.ap.m;
-  const long long row0 = (long long)blockIdx.x * G;
+  const long long row0 = bid * G;
   const bool even = (L & 1) == 0;
   const int total = nc * G2 * H;
   const FDiv fG2H(G2 * H), fH(H), fGL(G * L), fL(L);
@@ -629,13 +653,29 @@ __global__ void __launch_bounds__(kPassThreads) k_last_inv(const LastArgs<R> a0)
       if constexpr (EPI == EPI_CGF) acc.add(q);
     }
     const double bs = block_sum(acc.value());
-    if (threadIdx.x == 0) a.partial[blockIdx.x] = bs;
+    if (threadIdx.x == 0) a.partial[bid] = bs;
     CGState *st = const_cast<CGState *>(a.st);
-    if (cg_last_block(st)) {
-      if constexpr (EPI == EPI_CG) cg_alpha_step(st, a.partial, gridDim.x);
-      else cg_beta_step(st, a.partial, gridDim.x);
+    if (cg_last_block(st, nblk)) {
+      if constexpr (EPI == EPI_CG) cg_alpha_step(st, a.partial, nblk);
+      else cg_beta_step(st, a.partial, nblk);
     }
   }
+}
+
+template <typename R, int EPI, int D>
+__global__ void __launch_bounds__(kPassThreads) k_last_inv(const LastArgs<R> a0) {
+  dep_wait();
+  LastArgs<R> a = a0;
+  a.bind();
+  last_inv_body<R, EPI, D>(a, blockIdx.x, (int)gridDim.x);
+}
+
+template <typename R, int EPI, int D>
+__global__ void __launch_bounds__(kPassThreads) k_last_inv_g(const LastArgs<R> *tab, const int *blk0, int B) {
+  dep_wait();
+  const int b = group_problem(blk0, B);
+  const LastArgs<R> a = tab[b];
+  last_inv_body<R, EPI, D>(a, blockIdx.x - blk0[b], blk0[b + 1] - blk0[b]);
 }
 
 // ------------------------------------------------------------ pass "axis"
@@ -649,19 +689,13 @@ template <typename R> struct AxisArgs {
 };
 
 template <typename R, bool INV>
-__global__ void __launch_bounds__(kPassThreads) k_axis(const AxisArgs<R> a0) {
-  dep_wait();
+__device__ __forceinline__ void axis_body(const AxisArgs<R> &a, long long bid) {
   using T = typename V2<R>::T;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T *buf = reinterpret_cast<T *>(smem_raw);
-  AxisArgs<R> a = a0;
-  if (a0.batch) {
-    a.spec = a0.batch[blockIdx.y].spec;
-    a.st = a0.batch[blockIdx.y].st;
-  }
   if (a.st && !a.st->active) return;
-  const int tile = blockIdx.x % a.ntiles;
-  const long long batch = blockIdx.x / a.ntiles;
+  const int tile = (int)(bid % a.ntiles);
+  const long long batch = bid / a.ntiles;
   const int Tt = a.T;
   T *buf2 = buf + (size_t)Tt * a.ap.m;
   T *base = a.spec + batch * a.sb;
@@ -695,6 +729,25 @@ __global__ void __launch_bounds__(kPassThreads) k_axis(const AxisArgs<R> a0) {
     const long long pos = pos0 + t;
     if (pos < a.inner) base[e * a.se + pos] = res[idx];
   }
+}
+
+template <typename R, bool INV>
+__global__ void __launch_bounds__(kPassThreads) k_axis(const AxisArgs<R> a0) {
+  dep_wait();
+  AxisArgs<R> a = a0;
+  if (a0.batch) {
+    a.spec = a0.batch[blockIdx.y].spec;
+    a.st = a0.batch[blockIdx.y].st;
+  }
+  axis_body<R, INV>(a, blockIdx.x);
+}
+
+template <typename R, bool INV>
+__global__ void __launch_bounds__(kPassThreads) k_axis_g(const AxisArgs<R> *tab, const int *blk0, int B) {
+  dep_wait();
+  const int b = group_problem(blk0, B);
+  const AxisArgs<R> a = tab[b];
+  axis_body<R, INV>(a, blockIdx.x - blk0[b]);
 }
 
 // ------------------------------------------------------------ Green operators
@@ -773,21 +826,15 @@ template <typename R> struct GreenArgs {
 };
 
 template <typename R, int MODE, int D>
-__global__ void __launch_bounds__(kPassThreads) k_green(const GreenArgs<R> a0) {
-  dep_wait();
+__device__ __forceinline__ void green_body(const GreenArgs<R> &a, long long bid) {
   using T = typename V2<R>::T;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T *buf = reinterpret_cast<T *>(smem_raw);
-  GreenArgs<R> a = a0;
-  if (a0.batch) {
-    a.spec = a0.batch[blockIdx.y].spec;
-    a.st = a0.batch[blockIdx.y].st;
-  }
   if (a.st && !a.st->active) return;
   const int Tt = a.T, nc = a.ncomp, n0 = a.n0;
   const int P = nc * Tt;
   T *buf2 = buf + (size_t)P * a.ap.m;
-  const long long rho0 = (long long)blockIdx.x * Tt;
+  const long long rho0 = bid * Tt;
   const int total = nc * n0 * Tt;
   const FDiv fT(Tt), fn0(n0);
   for (int i0 = threadIdx.x; i0 < total; i0 += kLoadBatch * blockDim.x) {
@@ -867,6 +914,25 @@ __global__ void __launch_bounds__(kPassThreads) k_green(const GreenArgs<R> a0) {
     const long long rho = rho0 + t;
     if (rho < a.Rr) a.spec[(long long)c * a.nk + e * a.Rr + rho] = cur[e * P + c * Tt + t];
   }
+}
+
+template <typename R, int MODE, int D>
+__global__ void __launch_bounds__(kPassThreads) k_green(const GreenArgs<R> a0) {
+  dep_wait();
+  GreenArgs<R> a = a0;
+  if (a0.batch) {
+    a.spec = a0.batch[blockIdx.y].spec;
+    a.st = a0.batch[blockIdx.y].st;
+  }
+  green_body<R, MODE, D>(a, blockIdx.x);
+}
+
+template <typename R, int MODE, int D>
+__global__ void __launch_bounds__(kPassThreads) k_green_g(const GreenArgs<R> *tab, const int *blk0, int B) {
+  dep_wait();
+  const int b = group_problem(blk0, B);
+  const GreenArgs<R> a = tab[b];
+  green_body<R, MODE, D>(a, blockIdx.x - blk0[b]);
 }
 
 }  // namespace musg

@@ -3,6 +3,8 @@
 #pragma once
 
 #include <algorithm>
+#include <cstring>
+#include <memory>
 #include <mutex>
 #include <set>
 #include <vector>
@@ -570,6 +572,187 @@ void tangent_operator(Spectral &sp, int tkind, const TangentData<R> &td, const R
   launch_inv<R, EPI_PLAIN, 0>(a, c, s);
 }
 
+// ------------------------------------------------------------------ grouped launches
+// Device tables of one grouped operator: per pass the problems' arguments and the
+// prefix sums of their blocks; one shared-memory size (the largest) and one block
+// size (the first problem's tuned one) per pass.
+struct GroupedOp {
+  int dim = 0, tkind = 0, gm = 0, B = 0, prec = 0;
+  int threads[3] = {0, 0, 0};
+  size_t smem[3] = {0, 0, 0};
+  int total[3] = {0, 0, 0};       // blocks of the last-axis, middle-axis and Green launches
+  std::vector<int> fwd_parts;     // per problem: the forward pass's per-warp partial sums
+  DevBuf last, axisf, axisi, green, blk;  // argument tables; blk: 3 x (B + 1) prefix sums
+};
+
+template <typename T> void upload_vec(DevBuf &d, const std::vector<T> &v) {
+  d.alloc(v.size() * sizeof(T));
+  MUSG_CUDA(cudaMemcpy(d.p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+}
+
+template <typename R> GroupedOp *grouped_op_create(const std::vector<GroupProblem> &probs, int tkind) {
+  auto op = std::make_unique<GroupedOp>();
+  const int B = (int)probs.size();
+  Spectral &s0 = *probs[0].sp;
+  op->dim = s0.g.dim;
+  op->tkind = tkind;
+  op->gm = green_mode_of(s0);
+  op->B = B;
+  op->prec = sizeof(R) == 8 ? 0 : 1;
+  std::vector<LastArgs<R>> last(B);
+  std::vector<AxisArgs<R>> axf(B), axi(B);
+  std::vector<GreenArgs<R>> grn(B);
+  std::vector<int> blk(3 * (B + 1), 0);
+  op->fwd_parts.resize(B);
+  for (int b = 0; b < B; ++b) {
+    Spectral &sp = *probs[b].sp;
+    if (sp.g.dim != op->dim || green_mode_of(sp) != op->gm || sp.ncomp != s0.ncomp)
+      throw Error(MUSG_ERR_ARGUMENT, "a grouped operator needs one dimension, projection and component count");
+    for (int k = 0; k < 3; ++k) {  // one block size per launch: the first problem's
+      sp.tune_threads[op->prec][k] = s0.tune_threads[op->prec][k];
+      sp.tune_bytes[op->prec][k] = s0.tune_bytes[op->prec][k];
+    }
+    // last axis
+    const Cfg c = last_cfg<R>(sp);
+    LastArgs<R> a = last_args<R>(sp, c);
+    a.st = probs[b].st;
+    a.r = static_cast<R *>(probs[b].r);
+    a.x = static_cast<R *>(probs[b].x);
+    a.p = static_cast<R *>(probs[b].p);
+    a.Ap = static_cast<R *>(probs[b].Ap);
+    a.partial = probs[b].partial;
+    memcpy(&a.td, probs[b].td, sizeof(a.td));
+    last[b] = a;
+    blk[b + 1] = blk[b] + c.blocks;
+    op->fwd_parts[b] = c.blocks * ((c.threads + 31) / 32);
+    op->smem[0] = std::max(op->smem[0], c.smem);
+    op->threads[0] = c.threads;
+    // middle axis (3-D): the generic kernel's arguments of run_axis
+    if (op->dim == 3) {
+      const long long inner = sp.g.nh, nbatch = (long long)sp.ncomp * sp.g.n[0];
+      const Cfg ca = axis_cfg<R>(sp, 1, inner, nbatch);
+      AxisArgs<R> x{};
+      x.ap = sp.ax[1].device<R>();
+      x.nax = sp.g.n[1];
+      x.T = ca.per;
+      x.ntiles = (int)((inner + ca.per - 1) / ca.per);
+      x.se = sp.g.nh;
+      x.inner = inner;
+      x.sb = (long long)sp.g.n[1] * sp.g.nh;
+      x.spec = spec_of<R>(sp);
+      x.st = probs[b].st;
+      axf[b] = x;
+      axi[b] = x;
+      blk[(B + 1) + b + 1] = blk[(B + 1) + b] + ca.blocks;
+      op->smem[1] = std::max(op->smem[1], ca.smem);
+      op->threads[1] = ca.threads;
+    }
+    // first axis and the Green operator: the generic kernel's arguments of run_green
+    const long long Rr = sp.g.nk / sp.g.n[0];
+    const Cfg cg = green_cfg<R>(sp, Rr);
+    GreenArgs<R> g{};
+    g.ap = sp.ax[0].device<R>();
+    g.n0 = sp.g.n[0];
+    g.T = cg.per;
+    g.ncomp = sp.ncomp;
+    g.n1 = sp.g.n[1];
+    g.nh = sp.g.nh;
+    g.Rr = Rr;
+    g.nk = sp.g.nk;
+    g.spec = spec_of<R>(sp);
+    g.xi0 = xi_of<R>(sp, 0);
+    g.xi1 = xi_of<R>(sp, 1);
+    g.xi2 = op->dim == 3 ? xi_of<R>(sp, 2) : nullptr;
+    auto nyq = [&](int d) { return (sp.allow_even && sp.g.n[d] % 2 == 0) ? sp.g.n[d] / 2 : -1; };
+    g.nyq0 = nyq(0);
+    g.nyq1 = nyq(1);
+    g.nyq2 = op->dim == 3 ? nyq(2) : -1;
+    g.norm = R(1.0 / (double)sp.g.npx);
+    g.st = probs[b].st;
+    grn[b] = g;
+    blk[2 * (B + 1) + b + 1] = blk[2 * (B + 1) + b] + cg.blocks;
+    op->smem[2] = std::max(op->smem[2], cg.smem);
+    op->threads[2] = cg.threads;
+  }
+  for (int k = 0; k < 3; ++k) op->total[k] = blk[k * (B + 1) + B];
+  upload_vec(op->last, last);
+  if (op->dim == 3) {
+    upload_vec(op->axisf, axf);
+    upload_vec(op->axisi, axi);
+  }
+  upload_vec(op->green, grn);
+  upload_vec(op->blk, blk);
+  return op.release();
+}
+
+template <typename R, int PRO, int D, int TK>
+void launch_fwd_g(const GroupedOp &op, cudaStream_t s) {
+  auto k = k_last_fwd_g<R, PRO, D, TK>;
+  allow_smem(k);
+  launch_pdl(k, dim3(op.total[0]), dim3(op.threads[0]), op.smem[0], s, op.last.as<const LastArgs<R>>(),
+             op.blk.as<const int>(), op.B);
+  MUSG_CHECK_LAUNCH();
+}
+
+template <typename R>
+void grouped_op_run(GroupedOp *op, const BatchVec<R> *xtab, long long nmax, int B, cudaStream_t s) {
+  constexpr int kPro = sizeof(R) == 4 ? PRO_CGF : PRO_CG;
+  constexpr int kEpi = sizeof(R) == 4 ? EPI_CGF : EPI_CG;
+  const int dim = op->dim, tk = op->tkind, Bp = op->B + 1;
+  const int *blk = op->blk.as<const int>();
+  // last-axis forward with the CG prologue
+#define MUSG_FWDG_CASE(DD, TT) \
+  if (dim == DD && tk == TT) { launch_fwd_g<R, kPro, DD, TT>(*op, s); goto fwd_done; }
+  MUSG_FWDG_CASE(2, TK_SMALL) MUSG_FWDG_CASE(2, TK_FINITE) MUSG_FWDG_CASE(2, TK_KPRIME) MUSG_FWDG_CASE(2, TK_MIXED)
+  MUSG_FWDG_CASE(3, TK_SMALL) MUSG_FWDG_CASE(3, TK_FINITE) MUSG_FWDG_CASE(3, TK_KPRIME) MUSG_FWDG_CASE(3, TK_MIXED)
+  MUSG_FWDG_CASE(2, TK_GSMALL) MUSG_FWDG_CASE(2, TK_GFINITE) MUSG_FWDG_CASE(3, TK_GSMALL) MUSG_FWDG_CASE(3, TK_GFINITE)
+  MUSG_FWDG_CASE(2, TK_FULL) MUSG_FWDG_CASE(3, TK_FULL)
+  if constexpr (sizeof(R) == 4) {
+    MUSG_FWDG_CASE(2, TK_FISO) MUSG_FWDG_CASE(3, TK_FISO)
+  }
+#undef MUSG_FWDG_CASE
+  throw Error(MUSG_ERR_ARGUMENT, "unsupported tangent kind");
+fwd_done:
+  // FP32: alpha from each problem's own partial sums (nparts < 0), x += alpha p
+  if constexpr (sizeof(R) == 4) cg_update_x_batch<R>(xtab, nmax, -1, B, s);
+  if (dim == 3) {
+    auto k = k_axis_g<R, false>;
+    allow_smem(k);
+    launch_pdl(k, dim3(op->total[1]), dim3(op->threads[1]), op->smem[1], s, op->axisf.as<const AxisArgs<R>>(),
+               blk + Bp, op->B);
+    MUSG_CHECK_LAUNCH();
+  }
+  {
+#define MUSG_GREENG(MODE, DD)                                                                                   \
+  {                                                                                                             \
+    auto k = k_green_g<R, MODE, DD>;                                                                            \
+    allow_smem(k);                                                                                              \
+    launch_pdl(k, dim3(op->total[2]), dim3(op->threads[2]), op->smem[2], s, op->green.as<const GreenArgs<R>>(), \
+               blk + 2 * Bp, op->B);                                                                            \
+  }
+    if (op->gm == GM_SMALL && dim == 2) MUSG_GREENG(GM_SMALL, 2)
+    else if (op->gm == GM_SMALL) MUSG_GREENG(GM_SMALL, 3)
+    else if (dim == 2) MUSG_GREENG(GM_FINITE, 2)
+    else MUSG_GREENG(GM_FINITE, 3)
+#undef MUSG_GREENG
+    MUSG_CHECK_LAUNCH();
+  }
+  if (dim == 3) {
+    auto k = k_axis_g<R, true>;
+    allow_smem(k);
+    launch_pdl(k, dim3(op->total[1]), dim3(op->threads[1]), op->smem[1], s, op->axisi.as<const AxisArgs<R>>(),
+               blk + Bp, op->B);
+    MUSG_CHECK_LAUNCH();
+  }
+  {
+    auto k = dim == 2 ? k_last_inv_g<R, kEpi, 2> : k_last_inv_g<R, kEpi, 3>;
+    allow_smem(k);
+    launch_pdl(k, dim3(op->total[0]), dim3(op->threads[0]), op->smem[0], s, op->last.as<const LastArgs<R>>(), blk,
+               op->B);
+    MUSG_CHECK_LAUNCH();
+  }
+}
+
 // Autotuner: candidate (threads, shared-memory target) per pass, each timed with
 // CUDA events over `reps` launches on a scratch field; the fastest is kept.
 template <typename R> void spectral_autotune(Spectral &sp, cudaStream_t s, int effort) {
@@ -659,6 +842,8 @@ template <typename R> void spectral_autotune(Spectral &sp, cudaStream_t s, int e
                                     cudaStream_t);                                                 \
   template void spectral_autotune<R>(Spectral &, cudaStream_t, int);                               \
   template int cg_operator_batch<R>(Spectral &, int, const ProblemPtrs<R> *, const BatchVec<R> *, int,         \
-                                    cudaStream_t);
+                                    cudaStream_t);                                                             \
+  template GroupedOp *grouped_op_create<R>(const std::vector<GroupProblem> &, int);                         \
+  template void grouped_op_run<R>(GroupedOp *, const BatchVec<R> *, long long, int, cudaStream_t);
 
 }  // namespace musg

@@ -3,15 +3,17 @@
 Requests (one RVE each: grid, formulation, microstructure, load path) arrive over
 time.  The native server admits a request when a lane is free and its estimated
 device footprint fits the HBM budget next to everything already admitted; waiting
-requests of the same shape are taken together and solved as one batch (one launch
-per CG pass for all of them).  Each lane is a native host thread with its own CUDA
+requests of the same kind (dimension, formulation, law kind, load steps; grids within
+a factor 8 in pixels) are taken together and solved as one batch (one launch per CG
+pass for all of them, grouped over different grids).  Each lane is a native host thread with its own CUDA
 stream, so admitted requests overlap on the device.  Fields and plastic state stay on
 the device for all load steps of a request; memory returns to the budget when the
 request completes.  Latency = completion - submission.
 
-Every request is computed by the same deterministic kernels whether it runs alone
-or in the mix (per-request reductions in a fixed order), which
-``tests/test_gpu_serving.py`` checks.
+A request batched with requests of its own grid is computed by the kernels of its
+solo solve in the same order (per-request reductions in a fixed order), so its result
+is the same bit for bit; batched with other grids it runs the generic pass kernels
+and its result equals the solo one within rounding (``tests/test_gpu_serving.py``).
 """
 from __future__ import annotations
 
@@ -118,7 +120,7 @@ def estimate_bytes(res, formulation, has_hep, precision='mixed', consistent=Fals
 
 
 class Server:
-    """Admission by HBM budget, native lanes on separate streams, same-shape batching.
+    """Admission by HBM budget, native lanes on separate streams, batching by kind.
     ``lanes=0`` runs nothing: ``_take`` / ``_release`` then step the admission by
     hand (host-side checks of the policy)."""
 
@@ -158,6 +160,12 @@ class Server:
     def close(self):
         L.check(L.lib().musg_server_close(self._h))
 
+    def cancel_waiting(self):
+        """Drop the requests not yet admitted (they complete unsolved); returns their number."""
+        n = C.c_longlong(0)
+        L.check(L.lib().musg_server_cancel_waiting(self._h, C.byref(n)))
+        return int(n.value)
+
     def start(self):
         """Lanes start with the server; kept for the call sequence of run_stream."""
 
@@ -194,6 +202,10 @@ class Server:
     @property
     def admitted_batches(self):
         return int(self._stats().batches)
+
+    def waiting(self):
+        """Requests submitted and not yet admitted."""
+        return int(self._stats().queued)
 
     # ------------------------------------------------------------------ admission by hand
     def _take(self):
@@ -279,28 +291,40 @@ def _smooth235(n):
     return n == 1
 
 
-def run_stream(requests, rate_hz, server, seed=12345):
+def run_stream(requests, rate_hz, server, seed=12345, deadline_s=None):
     """Feed requests open loop with Poisson arrivals (exponential gaps at rate_hz;
     rate_hz <= 0 submits them all at once), wait for all.  A request the server
     refuses at submission (larger than the HBM budget, invalid) counts as failed.
-    Throughput is over the wall time from the first submission to the last
+    With ``deadline_s``, no request is submitted later than that after the first
+    submission, and the requests still waiting for admission then are cancelled
+    (counted as not completed; ``offered`` counts the submitted ones).  Throughput is
+    succeeded requests over the wall time from the first submission to the last
     completion."""
     rng = np.random.default_rng(seed)
     server.start()
     refused = {}
     t0 = time.perf_counter()
     next_t = t0
+    offered = 0
     for req in requests:
         if rate_hz > 0:
             now = time.perf_counter()
             if next_t > now:
                 time.sleep(next_t - now)
             next_t += float(rng.exponential(1.0 / rate_hz))
+        if deadline_s is not None and time.perf_counter() - t0 > deadline_s:
+            break
+        offered += 1
         try:
             server.submit(req)
         except (L.CudaError, ValueError, RuntimeError) as e:
             refused[req.rid] = str(e)[:60]
     server.close()
+    cancelled = 0
+    if deadline_s is not None:
+        while time.perf_counter() - t0 < deadline_s and server.waiting() > 0:
+            time.sleep(0.05)
+        cancelled = server.cancel_waiting()
     server.join()
     wall = time.perf_counter() - t0
     res = server.results
@@ -316,9 +340,10 @@ def run_stream(requests, rate_hz, server, seed=12345):
         key = '%s: refused: %s' % (laws.get(rid, '?'), msg)
         failed[key] = failed.get(key, 0) + 1
     ok_lat = np.array([r.latency for r in res.values() if r.success]) if ok else np.zeros(1)
-    return {'requests': len(requests), 'succeeded': int(ok), 'refused': len(refused), 'wall_s': wall,
+    return {'requests': len(requests), 'offered': offered, 'succeeded': int(ok), 'refused': len(refused),
+            'cancelled': cancelled, 'wall_s': wall,
             'offered_rate_hz': float(rate_hz) if rate_hz > 0 else None,
-            'solves_per_s': len(requests) / wall, 'succeeded_per_s': int(ok) / wall, 'failed': failed,
+            'solves_per_s': offered / wall, 'succeeded_per_s': int(ok) / wall, 'failed': failed,
             'p50_ms': float(np.percentile(lat, 50) * 1e3), 'p99_ms': float(np.percentile(lat, 99) * 1e3),
             'p50_ms_succeeded': float(np.percentile(ok_lat, 50) * 1e3),
             'p99_ms_succeeded': float(np.percentile(ok_lat, 99) * 1e3),

@@ -129,9 +129,10 @@ def newton_cg(cell, load_steps, solver, newton_tol, equil_tol=None, verbose=0, *
     ``line_search=True`` (an extension, off by default) damps every Newton increment
     by a backtracking line search on the norm of the projected residual: F = F0 + λ δF
     with λ = 1, 1/2, ... until the norm falls below (1 - 1e-4 λ) of the current one
-    (or λ = 1/1024).  The convergence test still measures the full increment δF.  It
-    is what makes the consistent elasto-plastic tangent converge on heterogeneous
-    cells under large load increments."""
+    (or λ = 1/1024).  The convergence test still measures the full increment δF, and
+    a load step takes at most min(maxiter, 100) Newton iterations.  It is what makes
+    the consistent elasto-plastic tangent converge on heterogeneous cells under large
+    load increments."""
     L.check(L.lib().musg_solver_set_line_search(solver.handle, 1 if line_search else 0))
     return _newton('musg_newton_cg', cell, load_steps, solver, newton_tol, equil_tol, verbose, return_fields, kw)
 

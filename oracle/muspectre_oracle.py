@@ -930,7 +930,8 @@ def newton_cg(cell, load_steps, solver, newton_tol, equil_tol, verbose=0, line_s
     """solvers.cc:44-217.  ``load_steps``: one D×D matrix or a list of them.
     Returns a list of OptimizeResult for a list input, one result otherwise.
     ``line_search`` (an extension, off by default) damps each Newton increment by
-    :func:`_line_search`; the convergence test still measures the full increment δF."""
+    :func:`_line_search`; the convergence test still measures the full increment δF,
+    and a load step takes at most min(maxiter, 100) Newton iterations."""
     single = isinstance(load_steps, np.ndarray) and load_steps.ndim == 2
     steps = [np.asarray(load_steps, dtype=float)] if single else [np.asarray(s, dtype=float) for s in load_steps]
     d = cell.dim
@@ -973,7 +974,8 @@ def newton_cg(cell, load_steps, solver, newton_tol, equil_tol, verbose=0, line_s
 
         newt_iter = 0
         evaluated = False
-        while newt_iter < solver.get_maxiter() and not state['conv']:
+        newton_max = min(solver.get_maxiter(), 100) if line_search else solver.get_maxiter()
+        while newt_iter < newton_max and not state['conv']:
             if not evaluated:
                 P, _ = cell.evaluate_stress_tangent()
                 rhs = -P

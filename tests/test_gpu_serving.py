@@ -1,6 +1,8 @@
 """Serving: requests of mixed size and load case run concurrently (lanes on
-separate streams, same-shape requests batched) and each result equals the same
-request solved alone."""
+separate streams, requests of one kind batched, grids of different sizes in grouped
+launches) and each result equals the same request solved alone: bit for bit when it
+ran as a group of its own, within the mixed-precision bound (1e-6 relative
+homogenised stress, the same Newton step count) when it shared a batch."""
 import numpy as np
 import pytest
 
@@ -28,8 +30,9 @@ def test_same_alone_and_in_the_mix():
         a, m = alone[r.rid], srv.results[r.rid]
         assert a.success == m.success
         if a.success:
-            assert (a.nb_it, a.nb_fev) == (m.nb_it, m.nb_fev)
-            assert np.linalg.norm(a.stress - m.stress) <= 1e-12 * np.linalg.norm(a.stress)
+            assert a.nb_it == m.nb_it
+            tol = 1e-12 if m.batched_with == 1 else 1e-6
+            assert np.linalg.norm(a.stress - m.stress) <= tol * np.linalg.norm(a.stress), (r.rid, m.batched_with)
     assert stats['p99_ms'] >= stats['p50_ms'] > 0
 
 

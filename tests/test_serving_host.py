@@ -1,5 +1,5 @@
 """Host logic of the native request server (no GPU: servers without lanes run
-nothing): admission by HBM budget, same-shape batching, memory returned on
+nothing): admission by HBM budget, batching by kind, memory returned on
 completion, request validation, the config-5 request generator."""
 import numpy as np
 
@@ -54,17 +54,20 @@ def test_oversized_request_refused():
     assert srv._take()[0] is None
 
 
-def test_batches_keep_shape_and_law_kind():
-    """Only requests of one shape (grid, formulation, law kind, steps) share a batch."""
+def test_batches_keep_kind_and_similar_size():
+    """Requests of one kind (dimension, formulation, law kind, steps) share a batch,
+    grids included that differ within a factor 8 in pixels; another law kind or a much
+    larger grid waits for a batch of its own."""
     srv = serving.Server(hbm_budget_bytes=1 << 40, lanes=0, max_batch=8)
     srv.submit(_req(0, 64))
     srv.submit(_req(1, 64, hep=True))
     srv.submit(_req(2, 64))
     srv.submit(_req(3, 80))
+    srv.submit(_req(4, 256))                        # 16x the pixels of 64^2
     g, _ = srv._take()
-    assert g == [0, 2]
+    assert g == [0, 2, 3]
     assert srv._take()[0] == [1]
-    assert srv._take()[0] == [3]
+    assert srv._take()[0] == [4]
 
 
 def test_request_validation():
@@ -129,3 +132,19 @@ def test_stream_report_groups_failures_by_law():
         assert msg == 'Conjugate gradient has not converged.'
         assert set(law.split('+')) <= {'le1', 'le4', 'hep1'}
     assert st['peak_hbm_bytes'] == 123 and st['batches'] == 1
+
+
+def test_cancel_waiting_requests():
+    """Requests still waiting for admission are dropped on demand (a stream's
+    deadline): each completes unsolved with its own message; admitted ones are not
+    affected."""
+    srv = serving.Server(hbm_budget_bytes=1 << 40, lanes=0, max_batch=1)
+    for rid in range(3):
+        srv.submit(_req(rid, 64))
+    g, used = srv._take()
+    assert g == [0] and srv.waiting() == 2
+    assert srv.cancel_waiting() == 2 and srv.waiting() == 0
+    for rid in (1, 2):
+        r = srv.result(rid, timeout=1.0)
+        assert not r.success and 'cancelled' in r.message
+    assert srv._take()[0] is None
