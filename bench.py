@@ -378,43 +378,48 @@ def voronoi_config(mu, workloads, n=64):
 
 
 def serving_config(mu, nreq=2000, lanes=4, max_batch=8, budget=96 << 30, sweep_n=400, sample=20,
-                   deadline_s=150.0, sweep_deadline_s=40.0, sample_budget_s=60.0):
+                   window_s=120.0, sweep_window_s=30.0, sample_budget_s=60.0, sample_service_s=0.5,
+                   sample_timeout_s=15.0):
     """The serving stream: nreq seeded requests of mixed size, formulation, law and
     load path through the continuous-batching server (mixed precision).  Capacity: all
-    nreq submitted at once (open loop, far past saturation); requests still waiting
-    for admission deadline_s after the first submission are cancelled, so that the
-    leg stays within minutes (their count is reported; throughput counts succeeded
-    requests over the wall time).  Rate sweep: Poisson arrivals at 1/2, 1 and 2 times
-    that capacity for sweep_deadline_s each (from the first sweep_n requests), each on
-    a fresh server (succeeded solves/s, p50/p99 latency).  Accuracy: a seeded sample of up to `sample` served requests
-    solved again alone in FP64 (the plain method, whose parity with the oracle the
-    tests pin) within sample_budget_s; the homogenised-stress error of the served
-    mixed result against it."""
+    nreq submitted at once (open loop, far past saturation) and a measurement window
+    of window_s: then the requests still waiting are cancelled and the running ones
+    stopped, so the leg stays within minutes (their counts are reported; throughput
+    counts succeeded requests over the wall time).  Rate sweep: Poisson arrivals at
+    1/2, 1 and 2 times that capacity for sweep_window_s each (from the first sweep_n
+    requests), each on a fresh server, ended the same way (succeeded solves/s, p50/p99
+    latency of the succeeded ones).  Accuracy: a seeded sample of up to `sample`
+    served requests, among those whose mixed solve took at most sample_service_s on
+    the device lane (an FP64 solve takes up to ~40x longer), solved again alone in
+    FP64 (the plain method, whose parity with the oracle the tests pin; each stopped
+    after sample_timeout_s), within sample_budget_s; the homogenised-stress error of
+    the served mixed result against it."""
     from muspectre_gb300 import serving
     t0 = time.perf_counter()
     reqs = [serving.c5_request(i, 1000 + i) for i in range(nreq)]
     t_gen = time.perf_counter() - t0
     srv = serving.Server(budget, lanes=lanes, max_batch=max_batch, precision='mixed')
-    cap = serving.run_stream(reqs, rate_hz=0, server=srv, deadline_s=deadline_s)
+    cap = serving.run_stream(reqs, rate_hz=0, server=srv, deadline_s=window_s, stop_running=True)
     mixed = dict(srv.results)
     del srv
-    progress('serving capacity run: %d succeeded, %d cancelled, %.1f s' % (cap['succeeded'], cap['cancelled'],
-                                                                           cap['wall_s']))
+    progress('serving capacity window: %d succeeded, %d cancelled, %.1f s' % (cap['succeeded'], cap['cancelled'],
+                                                                             cap['wall_s']))
     capacity = cap['succeeded_per_s']
     sweep = []
     for f in (0.5, 1.0, 2.0):
         s2 = serving.Server(budget, lanes=lanes, max_batch=max_batch, precision='mixed')
         st = serving.run_stream(reqs[:sweep_n], rate_hz=f * capacity, server=s2, seed=77,
-                                deadline_s=sweep_deadline_s)
+                                deadline_s=sweep_window_s, stop_running=True)
         sweep.append({'offered_hz': f * capacity, 'succeeded_per_s': st['succeeded_per_s'],
                       'p50_ms': st['p50_ms_succeeded'], 'p99_ms': st['p99_ms_succeeded'],
                       'succeeded': st['succeeded'], 'cancelled': st['cancelled'], 'offered': st['offered'],
-                      'batches': st['batches']})
+                      'stopped_running': sum(1 for r in s2.results.values() if 'while running' in r.message),
+                      'wall_s': st['wall_s'], 'batches': st['batches']})
         del s2
         progress('serving sweep at %.3g/s: %.3g succeeded/s' % (f * capacity, st['succeeded_per_s']))
     rng = np.random.default_rng(7)
     order = [int(i) for i in rng.permutation(nreq)]
-    errs = {}
+    errs, skipped = {}, 0
     t1 = time.perf_counter()
     for i in order:
         if len(errs) >= sample or time.perf_counter() - t1 > sample_budget_s:
@@ -422,16 +427,25 @@ def serving_config(mu, nreq=2000, lanes=4, max_batch=8, budget=96 << 30, sweep_n
         m = mixed.get(i)
         if m is None or not m.success:
             continue
-        r64 = serving.solve_alone(reqs[i], precision='fp64')
+        if m.service > sample_service_s:
+            skipped += 1
+            continue
+        r64 = serving.solve_alone(reqs[i], precision='fp64', timeout_s=sample_timeout_s)
         if r64.success:
             errs[i] = hom_err(m.stress, r64.stress)
     laws = [sorted({m[0] for m in r.materials}) for r in reqs]
-    cap.update({'arrivals': 'all %d submitted at once (open loop), waiting ones cancelled after %g s'
-                % (nreq, deadline_s), 'lanes': lanes, 'max_batch': max_batch,
+    svc = np.array([r.service for r in mixed.values() if r.success]) if mixed else np.zeros(1)
+    cap.update({'arrivals': 'all %d submitted at once (open loop); after %g s the waiting ones are cancelled and '
+                'the running ones stopped' % (nreq, window_s), 'lanes': lanes, 'max_batch': max_batch,
                 'hbm_budget_bytes': budget, 'request_generation_s': t_gen,
                 'elasto_plastic_requests': sum('hep1' in l for l in laws),
+                'stopped_running': sum(1 for r in mixed.values() if 'while running' in r.message),
+                'service_ms_succeeded': {'p50': float(np.percentile(svc, 50) * 1e3),
+                                         'p99': float(np.percentile(svc, 99) * 1e3)},
                 'rate_sweep': sweep,
                 'fp64_sample': {'requests': sorted(errs), 'compared': len(errs),
+                                'rule': 'seeded order, mixed service time <= %g s' % sample_service_s,
+                                'skipped_for_cost': skipped,
                                 'stress_rel_err_max': max(errs.values()) if errs else None,
                                 'stress_rel_err_median': float(np.median(list(errs.values()))) if errs else None,
                                 'within_1e-6': sum(e <= 1e-6 for e in errs.values())}})
@@ -583,7 +597,9 @@ def main():
     peak, peak_kind = measured_peaks()
     d2 = 9
     nk = (npx // w['res'][-1]) * (w['res'][-1] // 2 + 1)
-    tm = 4 * (9 + 2)  # F - I and lambda, mu per pixel (FP32); the operator rebuilds S from F
+    # algorithmic tangent data per pixel: F - I (FP32) and a 1-byte material index (the
+    # kernel reads per-pixel lambda, mu planes instead, 8 bytes; the operator rebuilds S)
+    tm = 4 * 9 + 1
     kern = {}
     for name, ms in prof.items():
         b = algorithmic_bytes(name, npx, nk, d2, 4, tm)

@@ -189,6 +189,12 @@ int musg_solver_destroy(musg_solver *solver);
  * solve stops at max(tol, inner_tol), default 1e-2 (the forcing term of an inexact
  * Newton method), and newton_cg refines in FP64 */
 int musg_solver_set_inner_tol(musg_solver *solver, double inner_tol);
+/* MUSG_PRECISION_MIXED only (no counterpart in the reference; on by default): newton_cg
+ * projects the first residual G(-P) of a load step in FP64 and every later one as
+ * G(rhs_prev - (P - P_prev)) in FP32, the previous residual minus the stress change
+ * since (one FP64 projection per load step instead of one per Newton iteration).
+ * enable = 0 projects every residual in FP64. */
+int musg_solver_set_incremental_residual(musg_solver *solver, int enable);
 /* newton_cg with a backtracking line search (no counterpart in the reference; off by
  * default): every Newton increment dF is applied as F0 + lam dF with lam = 1, 1/2, ...
  * until the norm of the projected residual G(-P) falls below (1 - 1e-4 lam) of the
@@ -196,6 +202,12 @@ int musg_solver_set_inner_tol(musg_solver *solver, double inner_tol);
  * step takes at most min(maxiter, 100) Newton iterations.  It lets the consistent
  * elasto-plastic tangent (HEP1 mode 2) converge on heterogeneous cells. */
 int musg_solver_set_line_search(musg_solver *solver, int enable);
+/* Cancellation of a running solve (no counterpart in the reference): flag points to
+ * a host int that another thread may set; while it is nonzero, SolverCG::solve,
+ * newton_cg and de_geus stop at their next check (after each replay of 16 CG
+ * iterations, before each Newton iteration) with MUSG_ERR_RUNTIME "cancelled while
+ * running".  NULL removes the flag; the int must outlive the solves that read it. */
+int musg_solver_set_stop_flag(musg_solver *solver, const int *flag);
 /* SolverBase::get_counter / reset_counter / has_converged (solver_base.hh:62-109) */
 int musg_solver_get_counter(musg_solver *solver, unsigned *counter);
 int musg_solver_reset_counter(musg_solver *solver);
@@ -237,6 +249,9 @@ int musg_batch_create(musg_cell **cells, int nb_cells, double tol, unsigned maxi
                       int precision, musg_batch **out);
 int musg_batch_destroy(musg_batch *batch);
 int musg_batch_set_inner_tol(musg_batch *batch, double inner_tol);
+/* musg_solver_set_stop_flag for a batch: checked after each graph replay and before
+ * each lockstep Newton iteration; the whole batch stops */
+int musg_batch_set_stop_flag(musg_batch *batch, const int *flag);
 int musg_batch_newton_cg(musg_batch *batch, const double *load_steps, int nb_steps,
                          double newton_tol, double equil_tol, musg_result_info *infos,
                          double *stresses);
@@ -281,6 +296,7 @@ typedef struct musg_server_result {
   unsigned nb_fev;            /* CG iterations of the last load step                 */
   double stress[9];           /* homogenised stress after the last step (column-major) */
   double latency_s;           /* completion - submission                             */
+  double service_s;           /* completion - admission (0 if never admitted)        */
   int batched_with;           /* requests of the batch it was solved in              */
   char message[64];
 } musg_server_result;
@@ -305,6 +321,10 @@ int musg_server_close(musg_server *srv);
  * with the message "cancelled before admission" (a deadline on a stream); running
  * groups finish.  *cancelled (may be NULL) receives their number. */
 int musg_server_cancel_waiting(musg_server *srv, long long *cancelled);
+/* asks every running group to stop: each ends at its next check (after a replay of 16
+ * CG iterations, before a Newton iteration) and completes, unsolved, with the message
+ * "cancelled while running".  *groups (may be NULL) receives the number signalled. */
+int musg_server_cancel_running(musg_server *srv, long long *groups);
 /* result of request id, waiting at most timeout_s seconds (MUSG_ERR_RUNTIME when it
  * is not done by then); a result can be fetched once */
 int musg_server_wait(musg_server *srv, long long id, double timeout_s, musg_server_result *out);

@@ -388,6 +388,9 @@ class SolverCG {
   void set_inner_tol(Real t) { check(musg_solver_set_inner_tol(h_, t)); }
   // newton_cg with a backtracking line search (extension; see musg_solver_set_line_search)
   void set_line_search(bool on) { check(musg_solver_set_line_search(h_, on ? 1 : 0)); }
+  // mixed precision: FP32 corrections of the Newton residual (extension; see
+  // musg_solver_set_incremental_residual)
+  void set_incremental_residual(bool on) { check(musg_solver_set_incremental_residual(h_, on ? 1 : 0)); }
   // SolverCG::solve: x = A^-1 rhs
   std::vector<Real> solve(const std::vector<Real> &rhs) {
     std::vector<Real> x(rhs.size());

@@ -55,7 +55,7 @@ class Request(C.Structure):
 class ServerResult(C.Structure):
     _fields_ = [('id', C.c_longlong), ('success', C.c_int), ('nb_steps_done', C.c_int), ('nb_it', C.c_uint),
                 ('nb_fev', C.c_uint), ('stress', C.c_double * 9), ('latency_s', C.c_double),
-                ('batched_with', C.c_int), ('message', C.c_char * 64)]
+                ('service_s', C.c_double), ('batched_with', C.c_int), ('message', C.c_char * 64)]
 
 
 class ServerStats(C.Structure):
@@ -102,6 +102,7 @@ _SIGNATURES = {
     'musg_solver_destroy': (C.c_int, [_P]),
     'musg_solver_set_inner_tol': (C.c_int, [_P, C.c_double]),
     'musg_solver_set_line_search': (C.c_int, [_P, C.c_int]),
+    'musg_solver_set_incremental_residual': (C.c_int, [_P, C.c_int]),
     'musg_probe_fp64_fma': (C.c_int, [C.POINTER(C.c_double)]),
     'musg_solver_get_counter': (C.c_int, [_P, C.POINTER(C.c_uint)]),
     'musg_solver_reset_counter': (C.c_int, [_P]),
@@ -132,6 +133,9 @@ _SIGNATURES = {
     'musg_server_submit': (C.c_int, [_P, C.POINTER(Request), _LL]),
     'musg_server_close': (C.c_int, [_P]),
     'musg_server_cancel_waiting': (C.c_int, [_P, _LL]),
+    'musg_server_cancel_running': (C.c_int, [_P, _LL]),
+    'musg_solver_set_stop_flag': (C.c_int, [_P, _I]),
+    'musg_batch_set_stop_flag': (C.c_int, [_P, _I]),
     'musg_server_wait': (C.c_int, [_P, C.c_longlong, C.c_double, C.POINTER(ServerResult)]),
     'musg_server_get_stats': (C.c_int, [_P, C.POINTER(ServerStats)]),
     'musg_server_destroy': (C.c_int, [_P]),

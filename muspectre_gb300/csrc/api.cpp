@@ -173,9 +173,12 @@ struct musg_cell {
   bool has_consistent = false;  // an HEP1 material with the consistent tangent: TK_FULL cell
   // device fields (FP64 component planes)
   DevBuf F, P, rhs, io, io2, F0;  // F0: the line search's Newton iterate
+  DevBuf Pk, dP32;                // the stress of the last projected residual; FP32 correction
+  bool residual_kept = false;     // Pk and rhs belong together (incremental residual)
   DevBuf mat, params, law_kind, Ctab64, Ctab32;
   bool has_generic = false;
   DevBuf lam64, mu64, lam32, mu32, eig;
+
   DevBuf Fprev[2], be[2], eps[2];
   DevBuf S64, S32, Kp64, Kp32, Fc64, Fc32, Kfull, Kt64, Kt32;
   DevBuf partial, scal;  // reduction scratch, small device scalars
@@ -482,6 +485,33 @@ struct musg_cell {
     for (int k = 0; k < 9; ++k) out[k] = k < D2 ? hscal[40 + k] : 0.0;
   }
 
+  // rhs = -G(P) for the current stress.  Incremental (the mixed path's default): the
+  // first residual after residual_kept is cleared is projected in FP64 and its P kept
+  // in Pk; each later one is G(rhs - (P - Pk)) projected in FP32 (rhs is in the range
+  // of G, so this is rhs - G(P - Pk) = -G(P)), and the new P is kept.  The FP32
+  // input is the previous residual minus the stress change since, whose size
+  // shrinks with the Newton increments: the result carries FP32 rounding of that
+  // change (not of P, whose mean and fluctuation are far larger), its part outside
+  // the range of G is rounding of the result itself (the fused CG iteration needs
+  // the right-hand side in that range), and the FP64 projections, bound by the FP64
+  // pipe, drop to one per load step.
+  void project_residual(bool incremental) {
+    if (!incremental || !residual_kept) {
+      spectral_project<double>(sp, P.as<double>(), rhs.as<double>(), -1.0, stream);
+      if (incremental) {
+        if (Pk.bytes < field_bytes()) Pk.alloc(field_bytes());
+        MUSG_CUDA(cudaMemcpyAsync(Pk.p, P.p, field_bytes(), cudaMemcpyDeviceToDevice, stream));
+        residual_kept = true;
+      }
+      return;
+    }
+    const long long n = nb_dof();
+    if (dP32.bytes < (size_t)n * sizeof(float)) dP32.alloc((size_t)n * sizeof(float));
+    residual_input(rhs.as<double>(), P.as<double>(), Pk.as<double>(), dP32.as<float>(), n, stream);
+    spectral_project<float>(sp, dP32.as<float>(), dP32.as<float>(), 1.0f, stream);
+    convert<double, float>(rhs.as<double>(), dP32.as<float>(), n, 1.0, stream);
+  }
+
   // host AoS vector -> device SoA planes (dst)
   void upload_field(const double *host, double *dst) {
     if (io.bytes < field_bytes()) io.alloc(field_bytes());
@@ -548,6 +578,10 @@ struct musg_solver {
   // newton_cg with a backtracking line search on the projected residual norm (an
   // extension, off by default; needed by the consistent elasto-plastic tangent)
   bool line_search = false;
+  // mixed precision: the Newton residual by FP32 corrections after one FP64 projection
+  // per load step (musg_cell::project_residual)
+  bool incremental_residual = true;
+  const int *stop = nullptr;  // musg_solver_set_stop_flag
 
   ~musg_solver() {
     if (exec) cudaGraphExecDestroy(exec);
@@ -692,6 +726,7 @@ struct musg_solver {
       }
       MUSG_CUDA(cudaMemcpyAsync(hst, st.p, sizeof(CGState), cudaMemcpyDeviceToHost, s));
       MUSG_CUDA(cudaStreamSynchronize(s));
+      check_stop(stop);
       if (verbose) {
         printf("  at CG step %d: |r|/|b| = %15g, cg_tol = %g\n", hst->iter - 1,
                std::sqrt(hst->rdr / hst->rhs_norm2), tol);
@@ -751,6 +786,7 @@ struct musg_batch {
   bool uniform = true;
   GroupedOp *gop = nullptr;
   long long nmax = 0;  // the largest cell's vector length
+  const int *stop = nullptr;  // musg_batch_set_stop_flag
 
   ~musg_batch() {
     if (gop) grouped_op_destroy(gop);
@@ -856,6 +892,7 @@ struct musg_batch {
       g_launches.fetch_add(graph_nodes);
       MUSG_CUDA(cudaMemcpyAsync(hst, states.p, B() * sizeof(CGState), cudaMemcpyDeviceToHost, stream));
       MUSG_CUDA(cudaStreamSynchronize(stream));
+      check_stop(stop);
       bool any = false;
       for (int b = 0; b < B(); ++b) any = any || hst[b].active;
       if (!any) break;
@@ -948,6 +985,8 @@ void newton_cg_impl(musg_cell *cell, const double *steps, int nsteps, musg_solve
     for (int k = 0; k < D2; ++k) delta[k] = macro[k] - previous[k];
     double *ddelta = c.put_matrix(delta.data(), 16);
     if (!geus) add_macro(c.F.as<double>(), ddelta, D2, c.npx, s);
+    c.residual_kept = false;  // the load step's first residual is projected in FP64
+    const bool incremental = solver->precision == MUSG_PRECISION_MIXED && solver->incremental_residual;
     std::string message = "Has not converged";
     double incr_norm = 2 * newton_tol, grad_norm = 1, stress_norm = 2 * equil_tol;
     bool has_converged = false;
@@ -966,6 +1005,7 @@ void newton_cg_impl(musg_cell *cell, const double *steps, int nsteps, musg_solve
     // kLineSearchNewtonMax iterations per load step
     const unsigned newton_max = solver->line_search ? std::min(solver->maxiter, kLineSearchNewtonMax) : solver->maxiter;
     for (; newt_iter < newton_max && !has_converged; ++newt_iter) {
+      check_stop(solver->stop);
       const bool first_geus = geus && newt_iter == 0;
       if (evaluated) {
         evaluated = false;
@@ -976,9 +1016,10 @@ void newton_cg_impl(musg_cell *cell, const double *steps, int nsteps, musg_solve
           fill_uniform(c.rhs.as<double>(), ddelta, D2, c.npx, s);
           tangent_operator<double>(c.sp, c.tkind, c.tangent<double>(), c.rhs.as<double>(), c.rhs.as<double>(), s);
           convert<double, double>(c.rhs.as<double>(), c.rhs.as<double>(), n, -1.0, s);
+          c.residual_kept = false;
         } else {
-          // rhs = -P, projected (FP64)
-          spectral_project<double>(c.sp, c.P.as<double>(), c.rhs.as<double>(), -1.0, s);
+          // rhs = -P, projected
+          c.project_residual(incremental);
         }
         dot_device<double, double>(c.rhs.as<double>(), c.rhs.as<double>(), n, c.partial.as<double>(), dscal + 32, s);
         MUSG_CUDA(cudaMemcpyAsync(c.hscal + 32, dscal + 32, sizeof(double), cudaMemcpyDeviceToHost, s));
@@ -1003,7 +1044,7 @@ void newton_cg_impl(musg_cell *cell, const double *steps, int nsteps, musg_solve
             newton_trial<double>(c.F.as<double>(), c.F0.as<double>(), solver->x.as<double>(), lam, n,
                                  c.partial.as<double>(), dscal + 34, s);
           c.evaluate(false);
-          spectral_project<double>(c.sp, c.P.as<double>(), c.rhs.as<double>(), -1.0, s);
+          c.project_residual(incremental);
           dot_device<double, double>(c.rhs.as<double>(), c.rhs.as<double>(), n, c.partial.as<double>(), dscal + 32, s);
           MUSG_CUDA(cudaMemcpyAsync(c.hscal + 32, dscal + 32, 4 * sizeof(double), cudaMemcpyDeviceToHost, s));
           MUSG_CUDA(cudaStreamSynchronize(s));
@@ -1103,8 +1144,10 @@ void batch_newton_impl(musg_batch *batch, const double *steps, int nsteps, doubl
       add_macro(c.F.as<double>(), c.put_matrix(delta.data(), 16), D2, c.npx, s);
       previous[b].assign(macro, macro + D2);
       running[b] = 1;
+      c.residual_kept = false;
     }
     for (;;) {
+      check_stop(bt.stop);
       // Newton iteration: evaluate, residual, convergence (per cell)
       std::vector<char> solve_it(B, 0);
       bool any = false;
@@ -1115,7 +1158,7 @@ void batch_newton_impl(musg_batch *batch, const double *steps, int nsteps, doubl
         }
         musg_cell &c = *bt.cells[b];
         c.evaluate(false);
-        spectral_project<double>(c.sp, c.P.as<double>(), c.rhs.as<double>(), -1.0, s);
+        c.project_residual(bt.precision == MUSG_PRECISION_MIXED && bt.solvers[b]->incremental_residual);
         dot_device<double, double>(c.rhs.as<double>(), c.rhs.as<double>(), c.nb_dof(), c.partial.as<double>(),
                                    c.scal.as<double>() + 32, s);
         MUSG_CUDA(cudaMemcpyAsync(c.hscal + 32, c.scal.as<double>() + 32, sizeof(double), cudaMemcpyDeviceToHost, s));
@@ -1673,6 +1716,27 @@ int musg_solver_set_line_search(musg_solver *solver, int enable) {
   return guard([&] {
     require(solver, MUSG_ERR_ARGUMENT, "null solver");
     solver->line_search = enable != 0;
+  });
+}
+
+int musg_solver_set_stop_flag(musg_solver *solver, const int *flag) {
+  return guard([&] {
+    require(solver, MUSG_ERR_ARGUMENT, "null solver");
+    solver->stop = flag;
+  });
+}
+
+int musg_batch_set_stop_flag(musg_batch *batch, const int *flag) {
+  return guard([&] {
+    require(batch, MUSG_ERR_ARGUMENT, "null batch");
+    batch->stop = flag;
+  });
+}
+
+int musg_solver_set_incremental_residual(musg_solver *solver, int enable) {
+  return guard([&] {
+    require(solver, MUSG_ERR_ARGUMENT, "null solver");
+    solver->incremental_residual = enable != 0;
   });
 }
 

@@ -295,6 +295,17 @@ __global__ void k_newton_update(double *__restrict__ F, const R *__restrict__ x,
   if (threadIdx.x == 0) partial[nparts + blockIdx.x] = s2;
 }
 
+// the input of the next residual's FP32 projection: d = rhs - (P - Pk) (the previous
+// residual minus the stress change since), and the new stress kept: Pk = P
+__global__ void k_residual_input(const double *__restrict__ rhs, const double *__restrict__ P,
+                                 double *__restrict__ Pk, float *__restrict__ d, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const double v = P[i];
+    d[i] = (float)(rhs[i] - (v - Pk[i]));
+    Pk[i] = v;
+  }
+}
+
 // line-search trial F = F0 + lam x; partial sums of x.x (the full Newton increment)
 // and F.F
 template <typename R>
@@ -323,6 +334,11 @@ __global__ void k_sum2_to(const double *partial, int nparts, double *out) {
     out[0] = a;
     out[1] = b;
   }
+}
+
+void residual_input(const double *rhs, const double *P, double *Pk, float *d, long long n, cudaStream_t s) {
+  k_residual_input<<<reduce_blocks(n), kRedThreads, 0, s>>>(rhs, P, Pk, d, n);
+  MUSG_CHECK_LAUNCH();
 }
 
 template <typename R>

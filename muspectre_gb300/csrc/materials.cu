@@ -379,8 +379,11 @@ __global__ void __launch_bounds__(kMatThreads) k_material(const MaterialArgs a, 
       for (int i = 0; i < D; ++i) dd += tau_d(i, j) * tau_d(j, i);
     const double tau_eq = sqrt(3 * .5 * dd);
     M<D> Nst;
+    // the consistent mode takes N = 0 for a deviator-free tau* (e.g. F = I), where the
+    // reference's 0/0 gives NaN; N only enters multiplied by dgamma = 0 there
+    const bool no_flow = consistent && !(tau_eq > 0.0);
 #pragma unroll
-    for (int k = 0; k < D2; ++k) Nst.a[k] = 3 * .5 * tau_d.a[k] / tau_eq;
+    for (int k = 0; k < D2; ++k) Nst.a[k] = no_flow ? 0.0 : 3 * .5 * tau_d.a[k] / tau_eq;
     double phi = tau_eq - mp.tau_y0 - mp.H * eps_old;
     phi = (phi < 0.0) ? 0.0 : phi;  // std::max(phi, 0.) keeps a NaN
     const double dgamma = phi / (mp.H + 3 * mu);

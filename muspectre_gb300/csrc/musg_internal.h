@@ -128,6 +128,12 @@ enum TangentKind : int {
                   // elasto-plastic tangent, and the elastic pixels of a cell that has it)
 };
 
+// A caller's stop flag (a host int another thread may set): nonzero ends a running
+// solve at its next check with MUSG_ERR_RUNTIME "cancelled while running".
+inline void check_stop(const int *flag) {
+  if (flag && __atomic_load_n(flag, __ATOMIC_RELAXED) != 0) throw Error(MUSG_ERR_RUNTIME, "cancelled while running");
+}
+
 // Device data the CG operator reads (precision R).
 template <typename R> struct TangentData {
   const R *lam = nullptr;   // [npx]
@@ -135,7 +141,7 @@ template <typename R> struct TangentData {
   const R *F = nullptr;     // [D*D][npx]  (finite strain): F in FP64, F - I in FP32
   const R *S = nullptr;     // [D*D][npx] PK2 stress (finite strain, isotropic)
   const R *Kp = nullptr;    // [D^3][npx]  (Kirchhoff tangent)
-  const uint8_t *mat = nullptr;      // [npx] material index (TK_MIXED)
+  const uint8_t *mat = nullptr;      // [npx] material index (TK_MIXED, C)
   const uint8_t *law_kind = nullptr; // [kMaxMaterials]: TK_FINITE or TK_KPRIME (TK_MIXED)
   const R *C = nullptr;     // [nmat][D^4] stiffness per material (TK_GSMALL / TK_GFINITE)
   const R *Kt = nullptr;    // [D^4][npx] per-pixel tangent planes, entry (i + D m) + D^2 (j + D n) (TK_FULL)
@@ -304,6 +310,9 @@ template <typename Ra, typename Rb>
 void dot_device(const Ra *a, const Rb *b, long long n, double *partial, double *out,
                 cudaStream_t s);
 // y += x (promoting), with the dots x.x and y.y (after the update) into out[0], out[1]
+// d = (float)(rhs - (P - Pk)), Pk = P: the FP32 input of the mixed path's
+// incremental Newton residual
+void residual_input(const double *rhs, const double *P, double *Pk, float *d, long long n, cudaStream_t s);
 template <typename R>
 void newton_update(double *F, const R *x, long long n, double *partial, double *out,
                    cudaStream_t s);

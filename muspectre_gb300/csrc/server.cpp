@@ -70,6 +70,7 @@ unsigned long long footprint(int dim, const int *res, int form, bool has_hep, bo
   b += tplanes * npx * 8;
   if (precision == MUSG_PRECISION_MIXED) {
     b += npx * 8 + d2 * nk * 8 + 3 * d2 * npx * 4;  // FP32 lambda/mu, spectrum, CG vectors x r p
+    b += d2 * npx * (8 + 4);                         // incremental residual: kept stress, FP32 change
     if (form == MUSG_FINITE_STRAIN) b += 2 * d2 * npx * 4;
     b += tplanes * npx * 4;
   } else {
@@ -198,6 +199,7 @@ struct musg_server {
   long long next_id = 1, submitted = 0, completed = 0, batches = 0;
   bool closed = false;
   std::vector<std::thread> threads;
+  std::vector<std::shared_ptr<int>> running;  // stop flags of the groups being solved
 
   // the admission step (caller holds mu)
   std::vector<std::shared_ptr<Req>> take(unsigned long long &used) {
@@ -227,7 +229,8 @@ struct musg_server {
     return group;
   }
 
-  std::vector<musg_server_result> run(const std::vector<std::shared_ptr<Req>> &group, cudaStream_t stream) {
+  std::vector<musg_server_result> run(const std::vector<std::shared_ptr<Req>> &group, cudaStream_t stream,
+                                      const int *stop) {
     const int n = (int)group.size();
     std::vector<musg_server_result> out(n);
     for (int k = 0; k < n; ++k) {
@@ -254,6 +257,7 @@ struct musg_server {
           throw Error(MUSG_ERR_RUNTIME, musg_last_error());
         // the consistent elasto-plastic tangent converges with the line search
         musg_solver_set_line_search(sv, group[0]->has_full ? 1 : 0);
+        musg_solver_set_stop_flag(sv, stop);
         rc[0] = musg_newton_cg(cells[0], group[0]->steps.data(), ns, sv, newton_tol, 0.0, 0, infos.data(), nullptr,
                                nullptr);
         if (rc[0] != MUSG_OK) err[0] = musg_last_error();
@@ -264,6 +268,7 @@ struct musg_server {
         musg_batch *b = nullptr;
         if (musg_batch_create(cells.data(), n, tol, maxiter, precision, &b) != MUSG_OK)
           throw Error(MUSG_ERR_RUNTIME, musg_last_error());
+        musg_batch_set_stop_flag(b, stop);
         const int brc = musg_batch_newton_cg(b, steps.data(), ns, newton_tol, 0.0, infos.data(), nullptr);
         const std::string berr = brc == MUSG_OK ? "" : musg_last_error();
         musg_batch_destroy(b);
@@ -318,8 +323,14 @@ struct musg_server {
         }
       }
       std::vector<musg_server_result> res;
+      const Clock::time_point ta = Clock::now();
+      auto stop = std::make_shared<int>(0);
+      {
+        std::lock_guard<std::mutex> lk(mu);
+        running.push_back(stop);
+      }
       if (stream) {
-        res = run(group, stream);
+        res = run(group, stream, stop.get());
       } else {
         res.resize(group.size());
         for (size_t k = 0; k < group.size(); ++k) {
@@ -332,8 +343,10 @@ struct musg_server {
       {
         std::lock_guard<std::mutex> lk(mu);
         in_use -= used;
+        running.erase(std::find(running.begin(), running.end(), stop));
         for (size_t k = 0; k < res.size(); ++k) {
           res[k].latency_s = std::chrono::duration<double>(t1 - group[k]->t0).count();
+          res[k].service_s = std::chrono::duration<double>(t1 - ta).count();
           done[res[k].id] = res[k];
         }
         completed += (long long)res.size();
@@ -437,6 +450,21 @@ int musg_server_cancel_waiting(musg_server *srv, long long *cancelled) {
     }
     srv->cv.notify_all();
     if (cancelled) *cancelled = n;
+  });
+}
+
+int musg_server_cancel_running(musg_server *srv, long long *groups) {
+  return guarded([&] {
+    need(srv != nullptr, MUSG_ERR_ARGUMENT, "null server");
+    long long n = 0;
+    {
+      std::lock_guard<std::mutex> lk(srv->mu);
+      for (const auto &f : srv->running) {
+        __atomic_store_n(f.get(), 1, __ATOMIC_RELAXED);
+        ++n;
+      }
+    }
+    if (groups) *groups = n;
   });
 }
 

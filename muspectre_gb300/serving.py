@@ -60,6 +60,7 @@ class Result:
     stress: np.ndarray          # homogenised PK1 / Cauchy stress of the last step (D×D)
     latency: float
     batched_with: int = 1
+    service: float = 0.0        # admission -> completion (seconds)
 
 
 def _native(req):
@@ -166,6 +167,13 @@ class Server:
         L.check(L.lib().musg_server_cancel_waiting(self._h, C.byref(n)))
         return int(n.value)
 
+    def cancel_running(self):
+        """Stop the groups being solved at their next check (they complete unsolved,
+        "cancelled while running"); returns the number of groups signalled."""
+        n = C.c_longlong(0)
+        L.check(L.lib().musg_server_cancel_running(self._h, C.byref(n)))
+        return int(n.value)
+
     def start(self):
         """Lanes start with the server; kept for the call sequence of run_stream."""
 
@@ -178,7 +186,7 @@ class Server:
         stress = np.array(out.stress[:d * d]).reshape(d, d).T
         res = Result(rid, bool(out.success), out.message.decode('utf-8', 'replace'), int(out.nb_it), int(out.nb_fev),
                      stress if out.success else np.full((d, d), np.nan), float(out.latency_s),
-                     int(out.batched_with))
+                     int(out.batched_with), float(out.service_s))
         self.results[rid] = res
         return res
 
@@ -222,12 +230,18 @@ class Server:
         L.check(L.lib().musg_server_release(self._h, C.c_ulonglong(int(used))))
 
 
-def solve_alone(req, tol=1e-8, maxiter=2000, newton_tol=1e-6, precision='mixed'):
+def solve_alone(req, tol=1e-8, maxiter=2000, newton_tol=1e-6, precision='mixed', timeout_s=None):
     """The reference point of the serving test: the request on its own (one lane,
-    no batching, nothing else running)."""
+    no batching, nothing else running).  With ``timeout_s`` a solve still running
+    then is cancelled (its result is unsolved, "cancelled while running")."""
     srv = Server(1 << 62, lanes=1, max_batch=1, precision=precision, tol=tol, maxiter=maxiter, newton_tol=newton_tol)
     srv.submit(req)
     srv.close()
+    if timeout_s is not None:
+        try:
+            return srv.result(req.rid, float(timeout_s))
+        except RuntimeError:
+            srv.cancel_running()
     return srv.result(req.rid)
 
 
@@ -291,15 +305,16 @@ def _smooth235(n):
     return n == 1
 
 
-def run_stream(requests, rate_hz, server, seed=12345, deadline_s=None):
+def run_stream(requests, rate_hz, server, seed=12345, deadline_s=None, stop_running=False):
     """Feed requests open loop with Poisson arrivals (exponential gaps at rate_hz;
     rate_hz <= 0 submits them all at once), wait for all.  A request the server
     refuses at submission (larger than the HBM budget, invalid) counts as failed.
     With ``deadline_s``, no request is submitted later than that after the first
     submission, and the requests still waiting for admission then are cancelled
-    (counted as not completed; ``offered`` counts the submitted ones).  Throughput is
-    succeeded requests over the wall time from the first submission to the last
-    completion."""
+    (counted as not completed; ``offered`` counts the submitted ones); with
+    ``stop_running`` the groups still being solved then are stopped too, so the
+    stream ends at the deadline (a measurement window).  Throughput is succeeded
+    requests over the wall time from the first submission to the last completion."""
     rng = np.random.default_rng(seed)
     server.start()
     refused = {}
@@ -325,6 +340,8 @@ def run_stream(requests, rate_hz, server, seed=12345, deadline_s=None):
         while time.perf_counter() - t0 < deadline_s and server.waiting() > 0:
             time.sleep(0.05)
         cancelled = server.cancel_waiting()
+        if stop_running:
+            server.cancel_running()
     server.join()
     wall = time.perf_counter() - t0
     res = server.results

@@ -8,7 +8,10 @@ return mapping) stays FP64.  The FP32 inner solve stops at max(tol, inner_tol)
 contracts the error by about inner_tol and the FP64 Newton loop refines to
 newton_tol, which takes fewer CG iterations in total than tight inner solves) and
 the FP64 Newton loop refines; for history-free materials the returned stress is
-evaluated at the returned strain.  ``newton_cg`` follows
+evaluated at the returned strain.  The Newton residual G(-P) is projected in FP64
+once per load step; later ones are the FP32 projection of the previous residual
+minus the stress change since (``incremental_residual=False`` projects every
+residual in FP64).  ``newton_cg`` follows
 src/solver/solvers.cc:44-217.
 """
 from __future__ import annotations
@@ -45,7 +48,8 @@ class SolverBase:
 class SolverCG(SolverBase):
     """SolverCG (src/solver/solver_cg.hh:51-106, solver_cg.cc:54-110)."""
 
-    def __init__(self, cell, tol, maxiter, verbose=False, precision='fp64', inner_tol=1e-2):
+    def __init__(self, cell, tol, maxiter, verbose=False, precision='fp64', inner_tol=1e-2,
+                 incremental_residual=True):
         if precision not in ('fp64', 'mixed'):
             raise ValueError("precision must be 'fp64' or 'mixed'")
         self.cell = cell
@@ -59,8 +63,10 @@ class SolverCG(SolverBase):
                                               C.byref(h)))
         self._h = h
         self.inner_tol = float(inner_tol)
+        self.incremental_residual = bool(incremental_residual)
         if precision == 'mixed':
             L.check(L.lib().musg_solver_set_inner_tol(self._h, self.inner_tol))
+            L.check(L.lib().musg_solver_set_incremental_residual(self._h, int(self.incremental_residual)))
 
     def __del__(self):
         h = getattr(self, '_h', None)
@@ -137,11 +143,14 @@ def newton_cg(cell, load_steps, solver, newton_tol, equil_tol=None, verbose=0, *
     return _newton('musg_newton_cg', cell, load_steps, solver, newton_tol, equil_tol, verbose, return_fields, kw)
 
 
-def de_geus(cell, load_steps, solver, newton_tol, equil_tol=None, verbose=0, *, return_fields=True, **kw):
+def de_geus(cell, load_steps, solver, newton_tol, equil_tol=None, verbose=0, *, return_fields=True,
+            line_search=False, **kw):
     """de_geus(cell, ΔF₀ | [ΔF...], solver, newton_tol, equil_tol, verbose=0)
     (bind_py_solvers.cc:108-138, solvers.cc:220-408): each load step starts with the
-    response to the macroscopic increment at the previous equilibrium."""
-    L.check(L.lib().musg_solver_set_line_search(solver.handle, 0))
+    response to the macroscopic increment at the previous equilibrium.
+    ``line_search=True`` (an extension, off by default) damps the later Newton
+    increments of a load step as in :func:`newton_cg`."""
+    L.check(L.lib().musg_solver_set_line_search(solver.handle, 1 if line_search else 0))
     return _newton('musg_de_geus', cell, load_steps, solver, newton_tol, equil_tol, verbose, return_fields, kw)
 
 

@@ -480,6 +480,11 @@ class MaterialHyperElastoPlastic1(Material):
             tau_d = tau_star - (tr / d)[:, None, None] * I
             tau_eq = np.sqrt(3 * 0.5 * np.einsum('pij,pji->p', tau_d, tau_d))
             N = 3 * 0.5 * tau_d / tau_eq[:, None, None]
+            if self.tangent == 'consistent':
+                # a deviator-free Kirchhoff stress (e.g. F = I) has no flow direction; the
+                # consistent mode takes N = 0 there (N only enters multiplied by Δγ = 0 or
+                # the plastic-only tangent term), where the reference's 0/0 gives NaN
+                N = np.where((tau_eq > 0)[:, None, None], N, 0.0)
             phi = np.maximum(tau_eq - self.tau_y0 - self.H * self._old(self.eps_p), 0.0)
             phi = np.where(np.isnan(tau_eq), np.nan, phi)  # std::max(NaN, 0) keeps NaN
             dgamma = phi / (self.H + 3 * self.mu)
@@ -1004,10 +1009,11 @@ def newton_cg(cell, load_steps, solver, newton_tol, equil_tol, verbose=0, line_s
     return results[0] if single else results
 
 
-def de_geus(cell, load_steps, solver, newton_tol, equil_tol, verbose=0):
+def de_geus(cell, load_steps, solver, newton_tol, equil_tol, verbose=0, line_search=False):
     """solvers.cc:220-408: Newton-Krylov of de Geus et al. (2017).  Per load step the
     first Newton iteration solves K δF = -G(K:ΔF̄) at the previous equilibrium
-    (:343-355) and then applies ΔF̄ + δF; later iterations are those of newton_cg."""
+    (:343-355) and then applies ΔF̄ + δF; later iterations are those of newton_cg
+    (``line_search`` as there, for the iterations after the first)."""
     single = isinstance(load_steps, np.ndarray) and load_steps.ndim == 2
     steps = [np.asarray(load_steps, dtype=float)] if single else [np.asarray(s, dtype=float) for s in load_steps]
     d = cell.dim
@@ -1045,8 +1051,11 @@ def de_geus(cell, load_steps, solver, newton_tol, equil_tol, verbose=0):
             return state['conv']
 
         newt_iter = 0
-        while newt_iter < solver.get_maxiter() and not state['conv']:
-            P, _ = cell.evaluate_stress_tangent()
+        evaluated = False
+        newton_max = min(solver.get_maxiter(), 100) if line_search else solver.get_maxiter()
+        while newt_iter < newton_max and not state['conv']:
+            if not evaluated:
+                P, _ = cell.evaluate_stress_tangent()
             if newt_iter == 0:
                 DeltaF = t2_to_vec(np.broadcast_to(macro - previous, (cell.n_px, d, d)).copy())
                 rhs = -cell.evaluate_projected_directional_stiffness(DeltaF)
@@ -1055,13 +1064,20 @@ def de_geus(cell, load_steps, solver, newton_tol, equil_tol, verbose=0):
                     break
                 incrF = solver.solve(rhs)
                 cell.F = cell.F + DeltaF
+                cell.F = cell.F + incrF
             else:
-                rhs = cell.apply_projection(-P)
-                stress_norm = math.sqrt(float(rhs @ rhs))
+                if not evaluated:
+                    rhs = cell.apply_projection(-P)
+                    stress_norm = math.sqrt(float(rhs @ rhs))
+                evaluated = False
                 if convergence_test():
                     break
                 incrF = solver.solve(rhs)
-            cell.F = cell.F + incrF
+                if line_search:
+                    rhs, stress_norm = _line_search(cell, incrF, stress_norm)
+                    evaluated = True
+                else:
+                    cell.F = cell.F + incrF
             incr_norm = math.sqrt(float(incrF @ incrF))
             grad_norm = math.sqrt(float(cell.F @ cell.F))
             if verbose > 0:

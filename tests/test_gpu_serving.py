@@ -87,3 +87,31 @@ def test_served_requests_vs_oracle():
             assert err < 1e-6, (r.rid, r.res, [x[0] for x in r.materials], err)
     finally:
         o.FFT_WORKERS = saved
+
+
+def test_cancel_running_request():
+    """A running solve stops at its next check when the server is asked to cancel the
+    running groups: it completes unsolved ("cancelled while running") well before it
+    would have finished, and the lane then solves the next request normally."""
+    import time
+    import muspectre_gb300 as mu
+    from muspectre_gb300 import serving, workloads
+    if mu.device_count() < 1:
+        pytest.fail('no CUDA device visible')
+    w = workloads.voronoi(n=64, nseeds=16, nsteps=20)
+    mats = [('hep1', (w[p]['E'], w[p]['nu'], w[p]['tau_y0'], w[p]['H'], 2.0)) for p in ('A', 'B')]
+    long_req = serving.Request(0, [64, 64, 64], int(mu.Formulation.finite_strain),
+                               (~w['phaseA']).astype(np.uint8), mats, w['steps'])
+    srv = serving.Server(1 << 36, lanes=1, max_batch=1)
+    srv.submit(long_req)
+    time.sleep(1.0)
+    t0 = time.perf_counter()
+    assert srv.cancel_running() == 1
+    r = srv.result(0, timeout=60.0)
+    assert not r.success and 'while running' in r.message, r.message
+    assert time.perf_counter() - t0 < 10.0
+    assert 0.5 < r.service < 20.0
+    small = serving.c5_request(1, 101, small=True)
+    srv.submit(small)
+    srv.close()
+    assert srv.result(1, timeout=120.0).success

@@ -109,3 +109,22 @@ def test_voronoi_ramp_solves_with_line_search():
     except o.ConvergenceError:
         diverged = True
     assert diverged
+
+
+def test_consistent_mode_at_identity_is_finite():
+    """At F = I the trial Kirchhoff stress has no deviator: the reference's flow
+    direction is 0/0 (NaN); the consistent mode takes N = 0 there, so P = 0 and the
+    tangent is the elastic one (what de_geus evaluates first)."""
+    mat = _material()
+    F = np.broadcast_to(np.eye(3), (6, 3, 3)).copy()
+    P, K = mat.evaluate(F, o.FINITE_STRAIN)
+    assert np.all(P == 0.0)
+    assert np.all(np.isfinite(K))
+    lam, mu = mat.lam, mat.mu
+    # the elastic tangent at F = I: lam tr(dF) I + mu (dF + dF^T)
+    for j in range(3):
+        for n in range(3):
+            dF = np.zeros((3, 3))
+            dF[j, n] = 1.0
+            ref = lam * np.trace(dF) * np.eye(3) + mu * (dF + dF.T)
+            assert np.allclose(K[0, :, :, j, n], ref, rtol=1e-12, atol=1e-3)

@@ -148,3 +148,11 @@ def test_cancel_waiting_requests():
         r = srv.result(rid, timeout=1.0)
         assert not r.success and 'cancelled' in r.message
     assert srv._take()[0] is None
+
+
+def test_cancel_running_without_lanes():
+    """A server without lanes has no running group to stop."""
+    srv = serving.Server(hbm_budget_bytes=1 << 40, lanes=0, max_batch=1)
+    srv.submit(_req(0, 64))
+    assert srv.cancel_running() == 0
+    assert srv.waiting() == 1
