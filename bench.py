@@ -378,16 +378,16 @@ def voronoi_config(mu, workloads, n=64):
 
 
 def serving_config(mu, nreq=2000, lanes=4, max_batch=8, budget=96 << 30, sweep_n=400, sample=20,
-                   window_s=120.0, sweep_window_s=30.0, sample_budget_s=60.0, sample_service_s=0.5,
-                   sample_timeout_s=15.0):
+                   window_s=75.0, sweep_window_s=20.0, sample_budget_s=45.0, sample_service_s=0.25,
+                   sample_timeout_s=10.0, sweep=(0.5, 1.0, 2.0, 4.0, 8.0)):
     """The serving stream: nreq seeded requests of mixed size, formulation, law and
     load path through the continuous-batching server (mixed precision).  Capacity: all
     nreq submitted at once (open loop, far past saturation) and a measurement window
     of window_s: then the requests still waiting are cancelled and the running ones
     stopped, so the leg stays within minutes (their counts are reported; throughput
     counts succeeded requests over the wall time).  Rate sweep: Poisson arrivals at
-    1/2, 1 and 2 times that capacity for sweep_window_s each (from the first sweep_n
-    requests), each on a fresh server, ended the same way (succeeded solves/s, p50/p99
+    the `sweep` multiples of that capacity for sweep_window_s each (from the first
+    sweep_n requests), each on a fresh server, ended the same way (succeeded solves/s, p50/p99
     latency of the succeeded ones).  Accuracy: a seeded sample of up to `sample`
     served requests, among those whose mixed solve took at most sample_service_s on
     the device lane (an FP64 solve takes up to ~40x longer), solved again alone in
@@ -405,8 +405,9 @@ def serving_config(mu, nreq=2000, lanes=4, max_batch=8, budget=96 << 30, sweep_n
     progress('serving capacity window: %d succeeded, %d cancelled, %.1f s' % (cap['succeeded'], cap['cancelled'],
                                                                              cap['wall_s']))
     capacity = cap['succeeded_per_s']
+    rates = sweep
     sweep = []
-    for f in (0.5, 1.0, 2.0):
+    for f in rates:
         s2 = serving.Server(budget, lanes=lanes, max_batch=max_batch, precision='mixed')
         st = serving.run_stream(reqs[:sweep_n], rate_hz=f * capacity, server=s2, seed=77,
                                 deadline_s=sweep_window_s, stop_running=True)

@@ -142,8 +142,20 @@ __device__ __forceinline__ int group_problem(const int *blk0, int B) {
 }
 
 __device__ __forceinline__ double sum_partials_fresh(const double *partial, int n) {
+  // eight independent loads in flight per thread; each thread still adds its entries
+  // in index order, so the sum is the same as one load at a time (tens of thousands of
+  // per-warp partials took one 1024-thread block 11.5 us, serialised on L2 latency)
+  const int nth = lin_nth();
+  int i = lin_tid();
   double v = 0.0;
-  for (int i = lin_tid(); i < n; i += lin_nth()) v += __ldcg(partial + i);
+  for (; i + 7 * nth < n; i += 8 * nth) {
+    double t[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) t[u] = __ldcg(partial + i + u * nth);
+#pragma unroll
+    for (int u = 0; u < 8; ++u) v += t[u];
+  }
+  for (; i < n; i += nth) v += __ldcg(partial + i);
   return block_sum(v);
 }
 
