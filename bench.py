@@ -378,7 +378,7 @@ def voronoi_config(mu, workloads, n=64):
 
 
 def serving_config(mu, nreq=2000, lanes=4, max_batch=8, budget=96 << 30, sweep_n=400, sample=20,
-                   window_s=75.0, sweep_window_s=20.0, sample_budget_s=45.0, sample_service_s=0.25,
+                   window_s=75.0, sweep_window_s=20.0, sample_budget_s=45.0, sample_max_cost=96 ** 3,
                    sample_timeout_s=10.0, sweep=(0.5, 1.0, 2.0, 4.0, 8.0)):
     """The serving stream: nreq seeded requests of mixed size, formulation, law and
     load path through the continuous-batching server (mixed precision).  Capacity: all
@@ -389,10 +389,11 @@ def serving_config(mu, nreq=2000, lanes=4, max_batch=8, budget=96 << 30, sweep_n
     the `sweep` multiples of that capacity for sweep_window_s each (from the first
     sweep_n requests), each on a fresh server, ended the same way (succeeded solves/s, p50/p99
     latency of the succeeded ones).  Accuracy: a seeded sample of up to `sample`
-    served requests, among those whose mixed solve took at most sample_service_s on
-    the device lane (an FP64 solve takes up to ~40x longer), solved again alone in
-    FP64 (the plain method, whose parity with the oracle the tests pin; each stopped
-    after sample_timeout_s), within sample_budget_s; the homogenised-stress error of
+    served requests, among those whose cost (pixels x load steps, x30 for the
+    elasto-plastic law) is at most sample_max_cost (an FP64 solve takes up to ~40x the
+    mixed one), solved again alone in FP64 (the plain method, whose parity with the
+    oracle the tests pin; each stopped after sample_timeout_s), within
+    sample_budget_s; the homogenised-stress error of
     the served mixed result against it."""
     from muspectre_gb300 import serving
     t0 = time.perf_counter()
@@ -428,7 +429,9 @@ def serving_config(mu, nreq=2000, lanes=4, max_batch=8, budget=96 << 30, sweep_n
         m = mixed.get(i)
         if m is None or not m.success:
             continue
-        if m.service > sample_service_s:
+        rq = reqs[i]
+        cost = int(np.prod(rq.res)) * len(rq.steps) * (30 if any(mm[0] == 'hep1' for mm in rq.materials) else 1)
+        if cost > sample_max_cost:
             skipped += 1
             continue
         r64 = serving.solve_alone(reqs[i], precision='fp64', timeout_s=sample_timeout_s)
@@ -445,7 +448,8 @@ def serving_config(mu, nreq=2000, lanes=4, max_batch=8, budget=96 << 30, sweep_n
                                          'p99': float(np.percentile(svc, 99) * 1e3)},
                 'rate_sweep': sweep,
                 'fp64_sample': {'requests': sorted(errs), 'compared': len(errs),
-                                'rule': 'seeded order, mixed service time <= %g s' % sample_service_s,
+                                'rule': 'seeded order, pixels x load steps (x30 elasto-plastic) <= %d'
+                                        % sample_max_cost,
                                 'skipped_for_cost': skipped,
                                 'stress_rel_err_max': max(errs.values()) if errs else None,
                                 'stress_rel_err_median': float(np.median(list(errs.values()))) if errs else None,

@@ -294,7 +294,8 @@ typedef struct musg_server_result {
   int nb_steps_done;
   unsigned nb_it;             /* Newton iterations of the last load step             */
   unsigned nb_fev;            /* CG iterations of the last load step                 */
-  double stress[9];           /* homogenised stress after the last step (column-major) */
+  double stress[9];           /* homogenised stress after the last step (column-major), at
+                                 the returned strain (elasto-plastic: the last evaluation) */
   double latency_s;           /* completion - submission                             */
   double service_s;           /* completion - admission (0 if never admitted)        */
   int batched_with;           /* requests of the batch it was solved in              */

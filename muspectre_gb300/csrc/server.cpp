@@ -286,6 +286,14 @@ struct musg_server {
         if (rc[k] != MUSG_OK) set_message(res, err[k]);
         else set_message(res, last.message);
         for (int c = 0; c < 9; ++c) res.stress[c] = 0.0;
+        // the homogenised stress at the returned strain: an FP64 newton_cg leaves the
+        // stress of its last evaluation, one Newton increment earlier, so history-free
+        // cells are evaluated once more (a mixed solve already did that)
+        if (res.success && precision == MUSG_PRECISION_FP64 && !group[k]->has_hep &&
+            musg_cell_evaluate_stress_tangent(cells[k], nullptr, nullptr) != MUSG_OK) {
+          res.success = 0;
+          set_message(res, musg_last_error());
+        }
         if (res.success && musg_cell_homogenised_stress(cells[k], res.stress) != MUSG_OK) {
           res.success = 0;
           set_message(res, musg_last_error());

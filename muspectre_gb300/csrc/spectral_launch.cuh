@@ -517,15 +517,16 @@ int cg_operator(Spectral &sp, int tkind, const TangentData<R> &td, const CGState
     run_axis<R>(sp, true, st, s);
     mark();
   }
+  int nb;
   if (greg) {
-    const int nb = last_cg_reg<R>(sp, tkind, a, ginv, true, s, 1);
-    mark();
-    return nb;
+    nb = last_cg_reg<R>(sp, tkind, a, ginv, true, s, 1);
+  } else {
+    if (sp.g.dim == 2) launch_inv<R, kEpi, 2>(a, c, s);
+    else launch_inv<R, kEpi, 3>(a, c, s);
+    nb = c.blocks;
   }
-  if (sp.g.dim == 2) launch_inv<R, kEpi, 2>(a, c, s);
-  else launch_inv<R, kEpi, 3>(a, c, s);
   mark();
-  return c.blocks;
+  return nb;
 }
 
 static_assert(sizeof(ProblemPtrs<float>) == sizeof(ProblemPtrsHost) &&
