@@ -264,8 +264,11 @@ template <int M> struct LastLayout {
 // forward with the CG prologue of the FP32 inner solve (PRO_CGF): p = -r + beta p
 // (p = -r on the first iteration), v = K:p per pixel, spectrum of v, and the per-warp
 // sums of p.v (cg_alpha finishes alpha = r.r / p.(K:p) from them).  FP32 only.
+// At most 72 registers (blocks of up to 512 threads still fit): the pass is bound by
+// load latency, and at 82 registers only five blocks of 144 threads shared an SM; six
+// took the 128^3 pass from 84.3 to 79.1 us (no spills for the isotropic tangents).
 template <int M, int D, int TK>
-__global__ void __launch_bounds__(512) k_last_fwd_reg(const LastArgs<float> a0) {
+__global__ void __maxnreg__(72) k_last_fwd_reg(const LastArgs<float> a0) {
   dep_wait();
   using R = float;
   using T = float2;
