@@ -318,11 +318,17 @@ struct musg_server {
     for (;;) {
       std::vector<std::shared_ptr<Req>> group;
       unsigned long long used = 0;
+      // the group's stop flag is registered in the same critical section that admits
+      // it, so musg_server_cancel_running reaches every admitted group
+      auto stop = std::make_shared<int>(0);
       {
         std::unique_lock<std::mutex> lk(mu);
         for (;;) {
           group = take(used);
-          if (!group.empty()) break;
+          if (!group.empty()) {
+            running.push_back(stop);
+            break;
+          }
           if (closed && queue.empty()) {
             if (stream) cudaStreamDestroy(stream);
             return;
@@ -332,11 +338,6 @@ struct musg_server {
       }
       std::vector<musg_server_result> res;
       const Clock::time_point ta = Clock::now();
-      auto stop = std::make_shared<int>(0);
-      {
-        std::lock_guard<std::mutex> lk(mu);
-        running.push_back(stop);
-      }
       if (stream) {
         res = run(group, stream, stop.get());
       } else {
