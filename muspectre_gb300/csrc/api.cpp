@@ -173,12 +173,11 @@ struct musg_cell {
   bool has_consistent = false;  // an HEP1 material with the consistent tangent: TK_FULL cell
   // device fields (FP64 component planes)
   DevBuf F, P, rhs, io, io2, F0;  // F0: the line search's Newton iterate
-  DevBuf Pk, dP32;                // the stress of the last projected residual; FP32 correction
+  DevBuf Pk, dP32;                // the stress of the last projected residual; FP32 projection input
   bool residual_kept = false;     // Pk and rhs belong together (incremental residual)
   DevBuf mat, params, law_kind, Ctab64, Ctab32;
   bool has_generic = false;
   DevBuf lam64, mu64, lam32, mu32, eig;
-
   DevBuf Fprev[2], be[2], eps[2];
   DevBuf S64, S32, Kp64, Kp32, Fc64, Fc32, Kfull, Kt64, Kt32;
   DevBuf partial, scal;  // reduction scratch, small device scalars
