@@ -156,3 +156,57 @@ def test_cancel_running_without_lanes():
     srv.submit(_req(0, 64))
     assert srv.cancel_running() == 0
     assert srv.waiting() == 1
+
+
+def test_stream_window_ends_at_the_deadline():
+    """run_stream with a deadline: nothing is submitted after it, the requests still
+    waiting then are cancelled, and with stop_running the running groups are stopped
+    too (a stand-in server that never finishes a request on its own; no GPU)."""
+    import time
+    reqs = [serving.c5_request(i, 3000 + i, small=True) for i in range(50)]
+
+    class SlowServer:
+        peak_in_use = 0
+        admitted_batches = 0
+
+        def __init__(self):
+            self.results, self.queue, self.calls = {}, [], []
+
+        def start(self):
+            pass
+
+        def submit(self, req):
+            self.queue.append(req.rid)
+
+        def close(self):
+            pass
+
+        def waiting(self):
+            return len(self.queue) - 1  # one request "running", the rest waiting
+
+        def cancel_waiting(self):
+            self.calls.append('waiting')
+            n = len(self.queue) - 1
+            for rid in self.queue[1:]:
+                self.results[rid] = serving.Result(rid, False, 'cancelled before admission', 0, 0,
+                                                   np.zeros((2, 2)), 0.0)
+            self.queue = self.queue[:1]
+            return n
+
+        def cancel_running(self):
+            self.calls.append('running')
+            rid = self.queue.pop()
+            self.results[rid] = serving.Result(rid, False, 'cancelled while running', 0, 0, np.zeros((2, 2)), 0.0)
+            return 1
+
+        def join(self):
+            assert not self.queue, 'a request would still be running'
+
+    srv = SlowServer()
+    t0 = time.perf_counter()
+    st = serving.run_stream(reqs, rate_hz=100.0, server=srv, seed=3, deadline_s=0.2, stop_running=True)
+    assert time.perf_counter() - t0 < 5.0
+    assert 0 < st['offered'] < len(reqs)
+    assert srv.calls == ['waiting', 'running']
+    assert st['succeeded'] == 0 and st['cancelled'] == st['offered'] - 1
+    assert sum(st['failed'].values()) == st['offered']
