@@ -65,3 +65,23 @@ def test_scaled_sample_matches_complete_solves():
             assert 0.65 < ratio < 1.35, (n, t_full, 1.0 / est['solves_per_s'])
     finally:
         o.FFT_WORKERS = saved
+
+
+def test_fused_iteration_bytes():
+    """The algorithmic bytes bench.py counts for the mixed CG iteration (its roofline
+    numerator): six passes moving 8 fields and 8 half spectra plus the tangent data, i.e.
+    16u + T_m with the half spectrum counted as a field (within 2/N at 128^3), against
+    19u + T_m for the unfused iteration (forward, update, three FFT passes, inverse)."""
+    sys.path.insert(0, ROOT)
+    import bench
+    n = 128
+    npx, nk, d2, s = n ** 3, n * n * (n // 2 + 1), 9, 4
+    u = npx * d2 * s
+    tm = 4 * 9 + 1
+    fused = ['last_axis_fwd_tangent_alpha', 'cg_update_x', 'axis1_fwd', 'green_axis0', 'axis1_inv',
+             'last_axis_inv_update_r']
+    unfused = ['last_axis_fwd_tangent', 'axis1_fwd', 'green_axis0', 'axis1_inv', 'last_axis_inv_dot', 'cg_update']
+    b_fused = sum(bench.algorithmic_bytes(k, npx, nk, d2, s, tm) for k in fused)
+    b_unfused = sum(bench.algorithmic_bytes(k, npx, nk, d2, s, tm) for k in unfused)
+    assert abs(b_fused - (16 * u + tm * npx)) <= 2 / n * 16 * u
+    assert abs(b_unfused - (19 * u + tm * npx)) <= 2 / n * 19 * u
